@@ -1,0 +1,589 @@
+// dpg.cu -- host side of the C ABI in include/dpg.h: contexts, device
+// tables, and the launch sequence of one batched expansion.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "dpg.h"
+#include "expand_kernels.cuh"
+
+using namespace dpg;
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct dpg_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  dpg_robot_desc robot{};
+  RobotParams rp{};
+  std::string err;
+
+  // primitives
+  bool have_prims = false;
+  int P = 0;
+  int64_t S = 0, A = 0;
+  std::vector<int32_t> h_len, h_order;
+  std::vector<int64_t> h_soff, h_aoff;
+  DevBuf len, soff, aoff, order, key32, kconst32, st64, st32, act64, pose32, pose64, pbox;
+
+  // environment
+  bool have_env = false;
+  int dim = 0;
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  int n_obs = 0;
+  DevBuf obs32, obs64;
+
+  // per-call arena
+  DevBuf x64, nkey32, noff32, mask, cnt, tot, pbase, ord_pbase, ord_ibase;
+  DevBuf p_node, p_prim, p_verdict, p_fi, p_end, p_gap, p_flags, p_recheck;
+  DevCounters *d_ctr = nullptr;
+  DevCounters *h_ctr = nullptr;  // pinned
+  int *h_abort = nullptr;        // mapped pinned
+  int *d_abort = nullptr;
+  cudaEvent_t ev[6] = {};
+  double timings[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+int fail(dpg_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                        \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail((ctx), e_ == cudaErrorMemoryAllocation ? DPG_ERR_OOM : DPG_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));             \
+  } while (0)
+
+int ensure(dpg_ctx *c, DevBuf &b, size_t bytes) {
+  if (b.bytes >= bytes && b.p) return DPG_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  size_t want = std::max<size_t>(bytes, 256);
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    return fail(c, DPG_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  b.bytes = want;
+  return DPG_OK;
+}
+
+void release(DevBuf &b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+template <class T> T *P_(DevBuf &b) { return static_cast<T *>(b.p); }
+
+bool kind_ok(int k) { return k >= DPG_ROBOT_UNICYCLE1 && k <= DPG_ROBOT_QUAD2D; }
+
+RobotParams to_params(const dpg_robot_desc &r) {
+  RobotParams p{};
+  p.dt = r.dt;
+  for (int i = 0; i < 4; i++) p.w[i] = r.w[i];
+  p.half_len = 0.5 * r.box[0];
+  p.half_wid = 0.5 * r.box[1];
+  p.hitch = r.hitch;
+  p.wheelbase = r.wheelbase;
+  p.radius = r.radius;
+  p.mass = r.mass;
+  p.lever = r.arm / std::sqrt(2.0);
+  p.t2t = r.t2t;
+  for (int i = 0; i < 3; i++) p.inertia[i] = r.inertia[i];
+  p.ang_gain = r.ang_gain;
+  p.g = r.g;
+  return p;
+}
+
+int pos_dim(int kind) { return kind == DPG_ROBOT_QUAD3D ? 3 : 2; }
+int key_dim(int kind) {
+  switch (kind) {
+    case DPG_ROBOT_UNICYCLE1: return Robot<DPG_ROBOT_UNICYCLE1>::KEYD;
+    case DPG_ROBOT_CAR1: return Robot<DPG_ROBOT_CAR1>::KEYD;
+    case DPG_ROBOT_QUAD2D: return Robot<DPG_ROBOT_QUAD2D>::KEYD;
+    default: return Robot<DPG_ROBOT_QUAD3D>::KEYD;
+  }
+}
+int off_dim(int kind) {
+  switch (kind) {
+    case DPG_ROBOT_QUAD2D: return 4;
+    case DPG_ROBOT_QUAD3D: return 6;
+    default: return 2;
+  }
+}
+bool is_rollout(int kind) { return kind == DPG_ROBOT_QUAD2D || kind == DPG_ROBOT_QUAD3D; }
+
+// dispatch a functor templated on the robot kind
+template <class F> void with_kind(int kind, F &&f) {
+  switch (kind) {
+    case DPG_ROBOT_UNICYCLE1: f(std::integral_constant<int, DPG_ROBOT_UNICYCLE1>{}); break;
+    case DPG_ROBOT_CAR1: f(std::integral_constant<int, DPG_ROBOT_CAR1>{}); break;
+    case DPG_ROBOT_QUAD3D: f(std::integral_constant<int, DPG_ROBOT_QUAD3D>{}); break;
+    case DPG_ROBOT_QUAD2D: f(std::integral_constant<int, DPG_ROBOT_QUAD2D>{}); break;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int dpg_abi_version(void) { return DPG_ABI_VERSION; }
+
+const char *dpg_errstr(int code) {
+  switch (code) {
+    case DPG_OK: return "ok";
+    case DPG_ERR_ARG: return "invalid argument";
+    case DPG_ERR_OOM: return "out of memory";
+    case DPG_ERR_CUDA: return "CUDA error";
+    case DPG_ERR_TIMEOUT: return "device wait timed out";
+    case DPG_ERR_ABORTED: return "aborted";
+    case DPG_ERR_CAPACITY: return "output capacity too small";
+    case DPG_ERR_STATE: return "invalid call order";
+    case DPG_ERR_NODEVICE: return "no usable CUDA device";
+  }
+  return "unknown error";
+}
+
+int dpg_robot_default(int32_t kind, dpg_robot_desc *r) {
+  if (!r || !kind_ok(kind)) return DPG_ERR_ARG;
+  std::memset(r, 0, sizeof(*r));
+  r->kind = kind;
+  r->g = 9.81;
+  switch (kind) {
+    case DPG_ROBOT_UNICYCLE1:
+      r->nx = 3; r->nu = 2; r->n_parts = 1; r->dt = 0.1;
+      r->w[0] = 1.0; r->w[1] = 0.5;
+      r->box[0] = 0.5; r->box[1] = 0.25;
+      break;
+    case DPG_ROBOT_CAR1:
+      r->nx = 4; r->nu = 2; r->n_parts = 2; r->dt = 0.1;
+      r->w[0] = 1.0; r->w[1] = 0.5; r->w[2] = 0.5;
+      r->box[0] = 0.5; r->box[1] = 0.25;
+      r->hitch = 0.5; r->wheelbase = 0.25;
+      break;
+    case DPG_ROBOT_QUAD3D:
+      r->nx = 13; r->nu = 4; r->n_parts = 1; r->dt = 0.01;
+      r->w[0] = 1.0; r->w[1] = 0.5; r->w[2] = 0.1; r->w[3] = 0.05;
+      r->radius = 0.1; r->mass = 0.034; r->arm = 0.046; r->t2t = 0.006;
+      r->inertia[0] = 16.571710e-6; r->inertia[1] = 16.655602e-6; r->inertia[2] = 29.261652e-6;
+      break;
+    case DPG_ROBOT_QUAD2D:
+      r->nx = 6; r->nu = 2; r->n_parts = 1; r->dt = 0.01;
+      r->w[0] = 1.0; r->w[1] = 0.5; r->w[2] = 0.2; r->w[3] = 0.1;
+      r->box[0] = 0.5; r->box[1] = 0.25;
+      r->ang_gain = 34.0;
+      break;
+  }
+  return DPG_OK;
+}
+
+int dpg_create(dpg_ctx **out, int device, const dpg_robot_desc *robot) {
+  if (!out || !robot || !kind_ok(robot->kind)) return DPG_ERR_ARG;
+  *out = nullptr;
+  dpg_robot_desc def;
+  dpg_robot_default(robot->kind, &def);
+  if (robot->nx != def.nx || robot->nu != def.nu || robot->n_parts != def.n_parts || !(robot->dt > 0))
+    return DPG_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return DPG_ERR_NODEVICE;
+  dpg_ctx *c = new (std::nothrow) dpg_ctx();
+  if (!c) return DPG_ERR_OOM;
+  c->device = device;
+  c->robot = *robot;
+  c->rp = to_params(*robot);
+  int rc = DPG_OK;
+  do {
+    if (cudaSetDevice(device) != cudaSuccess) { rc = DPG_ERR_NODEVICE; break; }
+    if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+      rc = DPG_ERR_NODEVICE; break;
+    }
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = DPG_ERR_CUDA; break; }
+    if (cudaMalloc(&c->d_ctr, sizeof(DevCounters)) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
+    if (cudaHostAlloc(&c->h_ctr, sizeof(DevCounters), cudaHostAllocDefault) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
+    if (cudaHostAlloc(&c->h_abort, sizeof(int), cudaHostAllocMapped) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
+    *c->h_abort = 0;
+    if (cudaHostGetDevicePointer(&c->d_abort, c->h_abort, 0) != cudaSuccess) { rc = DPG_ERR_CUDA; break; }
+    for (auto &e : c->ev)
+      if (cudaEventCreate(&e) != cudaSuccess) { rc = DPG_ERR_CUDA; break; }
+  } while (0);
+  if (rc != DPG_OK) {
+    dpg_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return DPG_OK;
+}
+
+void dpg_destroy(dpg_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  DevBuf *bufs[] = {&c->len, &c->soff, &c->aoff, &c->order, &c->key32, &c->kconst32, &c->st64,
+                    &c->st32, &c->act64, &c->pose32, &c->pose64, &c->pbox, &c->obs32, &c->obs64,
+                    &c->x64, &c->nkey32, &c->noff32, &c->mask, &c->cnt, &c->tot, &c->pbase,
+                    &c->ord_pbase, &c->ord_ibase, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
+                    &c->p_end, &c->p_gap, &c->p_flags, &c->p_recheck};
+  for (DevBuf *b : bufs) release(*b);
+  if (c->d_ctr) cudaFree(c->d_ctr);
+  if (c->h_ctr) cudaFreeHost(c->h_ctr);
+  if (c->h_abort) cudaFreeHost(c->h_abort);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char *dpg_last_error(const dpg_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const double *states,
+                          const double *actions) {
+  if (!c) return DPG_ERR_ARG;
+  if (P <= 0 || !len || !states || !actions) return fail(c, DPG_ERR_ARG, "upload_primitives: empty input");
+  const int nx = c->robot.nx, nu = c->robot.nu, kind = c->robot.kind;
+  c->h_len.assign(len, len + P);
+  c->h_soff.resize(P);
+  c->h_aoff.resize(P);
+  int64_t S = 0, A = 0;
+  for (int p = 0; p < P; p++) {
+    if (len[p] < 1 || len[p] > 32767) return fail(c, DPG_ERR_ARG, "upload_primitives: length out of [1, 32767]");
+    c->h_soff[p] = S;
+    c->h_aoff[p] = A;
+    S += len[p];
+    A += len[p] - 1;
+  }
+  c->h_order.resize(P);
+  std::iota(c->h_order.begin(), c->h_order.end(), 0);
+  std::stable_sort(c->h_order.begin(), c->h_order.end(),
+                   [&](int a, int b) { return c->h_len[a] > c->h_len[b]; });
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc;
+  const int pd = pos_dim(kind), kd = key_dim(kind), parts = c->robot.n_parts;
+  if ((rc = ensure(c, c->len, sizeof(int32_t) * P)) ||
+      (rc = ensure(c, c->soff, sizeof(int64_t) * P)) ||
+      (rc = ensure(c, c->aoff, sizeof(int64_t) * P)) ||
+      (rc = ensure(c, c->order, sizeof(int32_t) * P)) ||
+      (rc = ensure(c, c->key32, sizeof(float) * kd * P)) ||
+      (rc = ensure(c, c->kconst32, sizeof(float) * P)) ||
+      (rc = ensure(c, c->st64, sizeof(double) * nx * S)) ||
+      (rc = ensure(c, c->st32, sizeof(float) * nx * S)) ||
+      (rc = ensure(c, c->act64, sizeof(double) * nu * std::max<int64_t>(A, 1))) ||
+      (rc = ensure(c, c->pose32, sizeof(Pose<float>) * parts * S)) ||
+      (rc = ensure(c, c->pose64, sizeof(Pose<double>) * parts * S)) ||
+      (rc = ensure(c, c->pbox, sizeof(double) * 2 * pd * P)))
+    return rc;
+  cudaStream_t st = c->stream;
+  CUDA_TRY(c, cudaMemcpyAsync(c->len.p, len, sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->soff.p, c->h_soff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->aoff.p, c->h_aoff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->order.p, c->h_order.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->st64.p, states, sizeof(double) * nx * S, cudaMemcpyHostToDevice, st));
+  if (A > 0)
+    CUDA_TRY(c, cudaMemcpyAsync(c->act64.p, actions, sizeof(double) * nu * A, cudaMemcpyHostToDevice, st));
+  const RobotParams rp = c->rp;
+  with_kind(kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    if (is_rollout(KIND))
+      rollout_primitives<KIND><<<(P + 127) / 128, 128, 0, st>>>(rp, P, P_<int32_t>(c->len), P_<int64_t>(c->soff),
+                                                                 P_<int64_t>(c->aoff), P_<double>(c->act64),
+                                                                 P_<double>(c->st64));
+    build_poses<KIND><<<(unsigned)((S + 255) / 256), 256, 0, st>>>(rp, S, P_<double>(c->st64),
+                                                                  P_<Pose<double>>(c->pose64),
+                                                                  P_<Pose<float>>(c->pose32), P_<float>(c->st32));
+    build_keys<KIND><<<(P + 127) / 128, 128, 0, st>>>(rp, P, P_<int32_t>(c->len), P_<int64_t>(c->soff),
+                                                       P_<double>(c->st64), P_<float>(c->key32),
+                                                       P_<float>(c->kconst32), P_<double>(c->pbox));
+  });
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  c->P = P;
+  c->S = S;
+  c->A = A;
+  c->have_prims = true;
+  return DPG_OK;
+}
+
+int dpg_upload_env(dpg_ctx *c, int32_t dim, const double *lo, const double *hi, int32_t n_obs,
+                   const double *obs_lo, const double *obs_hi) {
+  if (!c) return DPG_ERR_ARG;
+  if (dim != pos_dim(c->robot.kind)) return fail(c, DPG_ERR_ARG, "upload_env: dim does not match the robot");
+  if (!lo || !hi || n_obs < 0 || (n_obs > 0 && (!obs_lo || !obs_hi)))
+    return fail(c, DPG_ERR_ARG, "upload_env: missing arrays");
+  const int max_obs = 4096;
+  if (n_obs > max_obs) return fail(c, DPG_ERR_ARG, "upload_env: more than 4096 obstacles");
+  for (int i = 0; i < dim; i++)
+    if (!(lo[i] <= hi[i])) return fail(c, DPG_ERR_ARG, "upload_env: bounds lo > hi");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  std::vector<float> o32;
+  std::vector<double> o64;
+  for (int o = 0; o < n_obs; o++) {
+    double cen[3], half[3];
+    for (int i = 0; i < dim; i++) {
+      const double a = obs_lo[(size_t)o * dim + i], b = obs_hi[(size_t)o * dim + i];
+      if (!(a <= b)) return fail(c, DPG_ERR_ARG, "upload_env: obstacle lo > hi");
+      cen[i] = 0.5 * (a + b);
+      half[i] = 0.5 * (b - a);
+    }
+    for (int i = 0; i < dim; i++) { o64.push_back(cen[i]); o32.push_back((float)cen[i]); }
+    for (int i = 0; i < dim; i++) { o64.push_back(half[i]); o32.push_back((float)half[i]); }
+  }
+  int rc;
+  const size_t n32 = std::max<size_t>(o32.size(), 1), n64 = std::max<size_t>(o64.size(), 1);
+  if ((rc = ensure(c, c->obs32, sizeof(float) * n32)) || (rc = ensure(c, c->obs64, sizeof(double) * n64)))
+    return rc;
+  if (n_obs > 0) {
+    CUDA_TRY(c, cudaMemcpy(c->obs32.p, o32.data(), sizeof(float) * o32.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->obs64.p, o64.data(), sizeof(double) * o64.size(), cudaMemcpyHostToDevice));
+  }
+  c->dim = dim;
+  for (int i = 0; i < 3; i++) { c->lo[i] = i < dim ? lo[i] : 0; c->hi[i] = i < dim ? hi[i] : 0; }
+  c->n_obs = n_obs;
+  c->have_env = true;
+  return DPG_OK;
+}
+
+int dpg_sync(dpg_ctx *c) {
+  if (!c) return DPG_ERR_ARG;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return DPG_OK;
+}
+
+int dpg_set_abort(dpg_ctx *c, int32_t flag) {
+  if (!c) return DPG_ERR_ARG;
+  *(volatile int *)c->h_abort = flag ? 1 : 0;
+  return DPG_OK;
+}
+
+void *dpg_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaHostAlloc(&p, std::max<size_t>(bytes, 1), cudaHostAllocDefault) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void dpg_host_free(void *p) {
+  if (p) cudaFreeHost(p);
+}
+
+int dpg_last_timings(const dpg_ctx *c, double *t, int32_t n) {
+  if (!c || !t || n < 0) return DPG_ERR_ARG;
+  const int k = std::min(n, 4);
+  for (int i = 0; i < k; i++) t[i] = c->timings[i];
+  return k;
+}
+
+int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double *x, dpg_expand_out *out) {
+  if (!c || !opts || !out) return DPG_ERR_ARG;
+  if (!c->have_prims || !c->have_env) return fail(c, DPG_ERR_STATE, "expand: upload primitives and env first");
+  if (N < 0 || (N > 0 && !x)) return fail(c, DPG_ERR_ARG, "expand: bad node array");
+  if (N > (int64_t)1 << 31) return fail(c, DPG_ERR_ARG, "expand: more than 2^31 nodes");
+  if (!(opts->radius >= 0) || (opts->precision != DPG_FP32 && opts->precision != DPG_FP64))
+    return fail(c, DPG_ERR_ARG, "expand: bad radius or precision");
+  if (out->capacity < 0 || out->capacity > (int64_t)0xffffffffLL)
+    return fail(c, DPG_ERR_ARG, "expand: capacity out of range");
+  if (*(volatile int *)c->h_abort) return fail(c, DPG_ERR_ABORTED, "expand: abort flag raised");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const int kind = c->robot.kind, nx = c->robot.nx, P = c->P;
+  const int kd = key_dim(kind), od = off_dim(kind);
+  const bool fp64 = opts->precision == DPG_FP64;
+  const int64_t cap = out->capacity;
+  const int Ppad = (P + 31) / 32 * 32;
+  const int64_t W = (N + 31) / 32;
+  const int64_t B = (N + kNNThreads - 1) / kNNThreads;
+  const size_t es_bytes = fp64 ? sizeof(double) : sizeof(float);
+  cudaStream_t st = c->stream;
+  int rc;
+  if ((rc = ensure(c, c->x64, sizeof(double) * nx * std::max<int64_t>(N, 1))) ||
+      (rc = ensure(c, c->nkey32, sizeof(float) * kd * std::max<int64_t>(N, 1))) ||
+      (rc = ensure(c, c->noff32, sizeof(float) * od * std::max<int64_t>(N, 1))) ||
+      (rc = ensure(c, c->mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(W, 1) * Ppad)) ||
+      (rc = ensure(c, c->cnt, sizeof(uint32_t) * (size_t)std::max<int64_t>(B, 1) * P)) ||
+      (rc = ensure(c, c->tot, sizeof(uint32_t) * P)) ||
+      (rc = ensure(c, c->pbase, sizeof(unsigned long long) * P)) ||
+      (rc = ensure(c, c->ord_pbase, sizeof(unsigned long long) * (P + 1))) ||
+      (rc = ensure(c, c->ord_ibase, sizeof(unsigned long long) * (P + 1))))
+    return rc;
+  // pair arrays: the caller's device arrays when given, else the arena
+  const bool dev_out = opts->out_on_device != 0;
+  const size_t capz = (size_t)std::max<int64_t>(cap, 1);
+  PairView pv_out{};
+  pv_out.cap = cap;
+  if (dev_out) {
+    if ((rc = ensure(c, c->p_node, 4 * capz)) || (rc = ensure(c, c->p_prim, 4 * capz))) return rc;
+    pv_out.node = out->node ? out->node : P_<uint32_t>(c->p_node);
+    pv_out.prim = out->prim ? out->prim : P_<uint32_t>(c->p_prim);
+    pv_out.verdict = out->verdict;
+    pv_out.first_invalid = out->first_invalid;
+    pv_out.end_state = out->end_state;
+    pv_out.min_gap = out->min_gap;
+    pv_out.flags = out->flags;
+  } else {
+    if ((rc = ensure(c, c->p_node, 4 * capz)) || (rc = ensure(c, c->p_prim, 4 * capz)) ||
+        (rc = ensure(c, c->p_verdict, capz)) || (rc = ensure(c, c->p_fi, 2 * capz)) ||
+        (rc = ensure(c, c->p_end, es_bytes * nx * capz)) || (rc = ensure(c, c->p_gap, 4 * capz)) ||
+        (rc = ensure(c, c->p_flags, capz)))
+      return rc;
+    pv_out.node = P_<uint32_t>(c->p_node);
+    pv_out.prim = P_<uint32_t>(c->p_prim);
+    pv_out.verdict = out->verdict ? P_<uint8_t>(c->p_verdict) : nullptr;
+    pv_out.first_invalid = out->first_invalid ? P_<int16_t>(c->p_fi) : nullptr;
+    pv_out.end_state = out->end_state ? c->p_end.p : nullptr;
+    pv_out.min_gap = out->min_gap ? P_<float>(c->p_gap) : nullptr;
+    pv_out.flags = out->flags ? P_<uint8_t>(c->p_flags) : nullptr;
+  }
+  if ((rc = ensure(c, c->p_recheck, 4 * capz))) return rc;
+  pv_out.recheck = P_<uint32_t>(c->p_recheck);
+
+  CUDA_TRY(c, cudaEventRecord(c->ev[0], st));
+  if (N > 0) {
+    if (opts->x_on_device)
+      CUDA_TRY(c, cudaMemcpyAsync(c->x64.p, x, sizeof(double) * nx * N, cudaMemcpyDeviceToDevice, st));
+    else
+      CUDA_TRY(c, cudaMemcpyAsync(c->x64.p, x, sizeof(double) * nx * N, cudaMemcpyHostToDevice, st));
+  }
+  CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), st));
+  CUDA_TRY(c, cudaEventRecord(c->ev[1], st));
+
+  PrimView pv{};
+  pv.P = P;
+  pv.S = c->S;
+  pv.len = P_<int32_t>(c->len);
+  pv.soff = P_<int64_t>(c->soff);
+  pv.order = P_<int32_t>(c->order);
+  pv.key32 = P_<float>(c->key32);
+  pv.kconst32 = P_<float>(c->kconst32);
+  pv.st64 = P_<double>(c->st64);
+  pv.st32 = P_<float>(c->st32);
+  pv.pose32 = P_<Pose<float>>(c->pose32);
+  pv.pose64 = P_<Pose<double>>(c->pose64);
+  pv.pbox = P_<double>(c->pbox);
+  NodeView nv{N, P_<double>(c->x64), P_<float>(c->nkey32), P_<float>(c->noff32)};
+  EnvView ev{};
+  ev.dim = c->dim;
+  for (int i = 0; i < 3; i++) { ev.lo[i] = c->lo[i]; ev.hi[i] = c->hi[i]; }
+  ev.n_obs = c->n_obs;
+  ev.obs32 = c->obs32.p;
+  ev.obs64 = c->obs64.p;
+  const RobotParams rp = c->rp;
+  const double band = opts->contact_band > 0 ? opts->contact_band : 1e-4;
+  const double ball_band = opts->ball_band > 0 ? opts->ball_band : 1e-5;
+  DevCounters *ctr = c->d_ctr;
+
+  CheckArgs ca{};
+  ca.rp = rp;
+  ca.pv = pv;
+  ca.nv = nv;
+  ca.ev = ev;
+  ca.out = pv_out;
+  ca.ord_pbase = P_<unsigned long long>(c->ord_pbase);
+  ca.ord_ibase = P_<unsigned long long>(c->ord_ibase);
+  ca.ctr = ctr;
+  ca.abort_flag = c->d_abort;
+  ca.band = fp64 ? 0.0 : band;
+
+  cudaError_t launch_err = cudaSuccess;
+  with_kind(kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    using R = Robot<KIND>;
+    if (N > 0) {
+      prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
+      nn_mask<KIND><<<(unsigned)B, kNNThreads, 0, st>>>(rp, pv, nv, (float)opts->radius, opts->radius,
+                                                       (float)ball_band, Ppad, P_<uint32_t>(c->mask),
+                                                       P_<uint32_t>(c->cnt), ctr);
+      nn_prefix<<<(P + 255) / 256, 256, 0, st>>>(P, (int)B, P_<uint32_t>(c->cnt), P_<uint32_t>(c->tot));
+    } else {
+      cudaMemsetAsync(c->tot.p, 0, sizeof(uint32_t) * P, st);
+    }
+    scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), P_<uint32_t>(c->tot),
+                                    P_<unsigned long long>(c->pbase), P_<unsigned long long>(c->ord_pbase),
+                                    P_<unsigned long long>(c->ord_ibase), cap, ctr);
+    if (N > 0) {
+      dim3 eg((unsigned)((Ppad / 32 + 7) / 8), (unsigned)B);
+      nn_emit<<<eg, 256, 0, st>>>(P, Ppad, W, P_<uint32_t>(c->mask), P_<uint32_t>(c->cnt),
+                                  P_<unsigned long long>(c->pbase), cap, pv_out.node, pv_out.prim);
+    }
+    cudaEventRecord(c->ev[2], st);
+    // exact check: persistent grid, obstacles in shared memory
+    const size_t obs_bytes32 = R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>);
+    const size_t obs_bytes64 = R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>);
+    if (fp64) {
+      auto kern = check_pairs<KIND, double, false>;
+      const size_t sm = obs_bytes64 * std::max(c->n_obs, 1);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
+      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+    } else {
+      auto kern = check_pairs<KIND, float, true>;
+      const size_t sm = obs_bytes32 * std::max(c->n_obs, 1);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
+      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+    }
+    cudaEventRecord(c->ev[3], st);
+    if (!fp64) {
+      auto rk = recheck_pairs<KIND>;
+      const size_t sm = obs_bytes64 * std::max(c->n_obs, 1);
+      cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      rk<<<c->sm_count * 2, kCheckThreads, sm, st>>>(ca);
+    }
+    cudaEventRecord(c->ev[4], st);
+    launch_err = cudaGetLastError();
+  });
+  if (launch_err != cudaSuccess)
+    return fail(c, DPG_ERR_CUDA, std::string("expand launch: ") + cudaGetErrorString(launch_err));
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_ctr, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  const DevCounters h = *c->h_ctr;
+  out->n_pairs = (int64_t)h.n_pairs;
+  out->n_scanned = N * (int64_t)P;
+  out->n_contact_recheck = (int64_t)h.n_recheck;
+  out->n_ball_recheck = (int64_t)h.n_ball_recheck;
+  if (h.status == DPG_ERR_ABORTED) return fail(c, DPG_ERR_ABORTED, "expand: aborted");
+  if ((int64_t)h.n_pairs > cap) return fail(c, DPG_ERR_CAPACITY, "expand: output capacity too small");
+  const int64_t np = (int64_t)h.n_pairs;
+  if (!dev_out && np > 0) {
+    struct { void *dst; void *src; size_t b; } cp[] = {
+        {out->node, c->p_node.p, 4}, {out->prim, c->p_prim.p, 4}, {out->verdict, c->p_verdict.p, 1},
+        {out->first_invalid, c->p_fi.p, 2}, {out->end_state, c->p_end.p, es_bytes * nx},
+        {out->min_gap, c->p_gap.p, 4}, {out->flags, c->p_flags.p, 1}};
+    for (auto &e : cp)
+      if (e.dst) CUDA_TRY(c, cudaMemcpyAsync(e.dst, e.src, e.b * np, cudaMemcpyDeviceToHost, st));
+  } else if (dev_out && np > 0) {
+    // node / prim live in the arena unless the caller gave arrays
+  }
+  CUDA_TRY(c, cudaEventRecord(c->ev[5], st));
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->timings[0] = ms;
+  cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); c->timings[1] = ms;
+  cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); c->timings[2] = ms;
+  float t_in = 0, t_out = 0;
+  cudaEventElapsedTime(&t_in, c->ev[0], c->ev[1]);
+  cudaEventElapsedTime(&t_out, c->ev[4], c->ev[5]);
+  c->timings[3] = t_in + t_out;
+  return DPG_OK;
+}
+
+}  // extern "C"

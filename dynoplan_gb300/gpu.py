@@ -1,0 +1,173 @@
+"""Python handle over the C ABI (include/dpg.h): one context per robot,
+primitive set and environment; ``expand`` runs the batched expansion.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import ExpandOpts, ExpandOut, RobotDesc, check
+
+VALID, COLLISION, OUT_OF_BOUNDS = 0, 1, 2
+
+
+def robot_desc(model) -> RobotDesc:
+    """dpg_robot_desc from a workloads.RobotModel (or the library default for
+    an int kind)."""
+    lib = _lib.load()
+    d = RobotDesc()
+    if isinstance(model, int):
+        check(lib.dpg_robot_default(model, C.byref(d)))
+        return d
+    check(lib.dpg_robot_default(model.kind, C.byref(d)))
+    d.dt = model.dt
+    for i in range(4):
+        d.w[i] = model.w[i]
+    d.box[0], d.box[1] = model.box
+    d.hitch, d.wheelbase, d.radius = model.hitch, model.wheelbase, model.radius
+    d.mass, d.arm, d.t2t = model.mass, model.arm, model.t2t
+    for i in range(3):
+        d.inertia[i] = model.inertia[i]
+    d.ang_gain, d.g = model.ang_gain, model.g
+    return d
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class PinnedArray:
+    """numpy view of a page-locked host buffer (dpg_host_alloc)."""
+
+    def __init__(self, shape, dtype):
+        lib = _lib.load()
+        self.dtype = np.dtype(dtype)
+        self.shape = tuple(np.atleast_1d(shape))
+        nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self._p = lib.dpg_host_alloc(max(nbytes, 1))
+        if not self._p:
+            raise MemoryError("dpg_host_alloc failed")
+        buf = (C.c_char * max(nbytes, 1)).from_address(self._p)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=int(np.prod(self.shape))).reshape(self.shape)
+
+    def free(self):
+        if self._p:
+            self.array = None
+            _lib.load().dpg_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class ExpandResult(dict):
+    """numpy arrays per pair: node, prim, verdict, first_invalid, end_state,
+    min_gap, flags; plus counters."""
+
+
+class Context:
+    """A dpg_ctx: robot + primitives + environment on one GPU."""
+
+    def __init__(self, model, device: int = 0):
+        self.lib = _lib.load()
+        self.model = model
+        self.desc = robot_desc(model)
+        self.nx, self.nu = self.desc.nx, self.desc.nu
+        h = C.c_void_p()
+        check(self.lib.dpg_create(C.byref(h), device, C.byref(self.desc)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dpg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload_primitives(self, prims):
+        length = np.ascontiguousarray(prims.length, dtype=np.int32)
+        states = np.ascontiguousarray(prims.states, dtype=np.float64)
+        actions = np.ascontiguousarray(prims.actions, dtype=np.float64)
+        if actions.size == 0:
+            actions = np.zeros((1, self.nu))
+        check(self.lib.dpg_upload_primitives(self.h, len(length), _ptr(length), _ptr(states),
+                                             _ptr(actions)), self.h)
+        self.P = len(length)
+
+    def upload_env(self, env):
+        lo = np.ascontiguousarray(env.lo, dtype=np.float64)
+        hi = np.ascontiguousarray(env.hi, dtype=np.float64)
+        olo = np.ascontiguousarray(env.obs_lo, dtype=np.float64).reshape(-1)
+        ohi = np.ascontiguousarray(env.obs_hi, dtype=np.float64).reshape(-1)
+        n = len(env.obs_lo)
+        check(self.lib.dpg_upload_env(self.h, len(lo), _ptr(lo), _ptr(hi), n,
+                                      _ptr(olo) if n else None, _ptr(ohi) if n else None), self.h)
+
+    def expand(self, x: np.ndarray, radius: float, precision: int = 0, capacity: int | None = None,
+               contact_band: float = 1e-4, ball_band: float = 1e-5, outputs=None) -> ExpandResult:
+        """Batched expand of the rows of x (N x nx), results in host arrays."""
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, self.nx)
+        N = len(x)
+        if capacity is None:
+            capacity = max(1024, N * 64)
+        opts = ExpandOpts(radius=radius, precision=precision, x_on_device=0, out_on_device=0,
+                          reserved=0, contact_band=contact_band, ball_band=ball_band)
+        while True:
+            es_dtype = np.float64 if precision == 1 else np.float32
+            o = outputs if outputs is not None else dict(
+                node=np.empty(capacity, np.uint32), prim=np.empty(capacity, np.uint32),
+                verdict=np.empty(capacity, np.uint8), first_invalid=np.empty(capacity, np.int16),
+                end_state=np.empty((capacity, self.nx), es_dtype),
+                min_gap=np.empty(capacity, np.float32), flags=np.empty(capacity, np.uint8))
+            out = ExpandOut(capacity=capacity)
+            for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap", "flags"):
+                setattr(out, k, _ptr(o[k]) if o.get(k) is not None else None)
+            rc = self.lib.dpg_expand(self.h, C.byref(opts), N, _ptr(x), C.byref(out))
+            if rc == _lib.DPG_ERR_CAPACITY and outputs is None:
+                capacity = int(out.n_pairs)
+                continue
+            check(rc, self.h)
+            break
+        n = int(out.n_pairs)
+        res = ExpandResult({k: (v[:n] if v is not None else None) for k, v in o.items()})
+        res["n_pairs"] = n
+        res["n_scanned"] = int(out.n_scanned)
+        res["n_contact_recheck"] = int(out.n_contact_recheck)
+        res["n_ball_recheck"] = int(out.n_ball_recheck)
+        return res
+
+    def expand_device(self, x_ptr: int, N: int, radius: float, out_ptrs: dict, capacity: int,
+                      precision: int = 0, contact_band: float = 1e-4, ball_band: float = 1e-5):
+        """Expand with the nodes and all outputs in device memory (raw device
+        pointers); returns the counters."""
+        opts = ExpandOpts(radius=radius, precision=precision, x_on_device=1, out_on_device=1,
+                          reserved=0, contact_band=contact_band, ball_band=ball_band)
+        out = ExpandOut(capacity=capacity)
+        for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap", "flags"):
+            setattr(out, k, C.c_void_p(out_ptrs[k]) if out_ptrs.get(k) else None)
+        check(self.lib.dpg_expand(self.h, C.byref(opts), N, C.c_void_p(x_ptr), C.byref(out)), self.h)
+        return dict(n_pairs=int(out.n_pairs), n_scanned=int(out.n_scanned),
+                    n_contact_recheck=int(out.n_contact_recheck), n_ball_recheck=int(out.n_ball_recheck))
+
+    def timings(self):
+        t = (C.c_double * 4)()
+        k = self.lib.dpg_last_timings(self.h, t, 4)
+        return list(t)[:k]
+
+    def set_abort(self, flag: bool):
+        check(self.lib.dpg_set_abort(self.h, 1 if flag else 0), self.h)

@@ -1,0 +1,176 @@
+/*
+ * dpg.h -- C ABI of dynoplan_gb300: the db-A* / iDb-A* node expansion on one
+ * GB300 (sm_103a).
+ *
+ * The boundary replaces, for a BATCH of frontier states, the reference pair
+ *
+ *   Expander::expand_lazy(Eigen::Ref<const VectorXd> x, std::vector<LazyTraj>&)
+ *       include/dynoplan/dbastar/dbastar.hpp:270-312
+ *   check_lazy_trajectory(LazyTraj&, Model_robot&, Time_benchmark&,
+ *                         TrajWrapper&, Ref<VectorXd>, check_state*, int*, bool)
+ *       include/dynoplan/dbastar/dbastar.hpp:334-339, src/dbastar/dbastar.cpp:391-490
+ *
+ * as called by the search loop at src/dbastar/dbastar.cpp:806-818: for every
+ * node x_n and every primitive p with d(canonical(x_n), start_p) <= radius
+ * (radius = alpha * delta, dbastar.cpp:585-586) it produces the transformed
+ * end state, the bounds/collision verdict and the first invalid state.
+ *
+ * Conventions
+ *   - Every function returns 0 on success or a negative DPG_ERR_* code; no
+ *     C++ exception crosses this boundary.  dpg_errstr() names a code and
+ *     dpg_last_error() gives the context's last message.
+ *   - A context belongs to one host thread at a time (the reference Expander
+ *     holds mutable scratch too, dbastar.hpp:233-313).  All device work of a
+ *     context runs on its own CUDA stream.
+ *   - Input arrays are copied; the caller keeps ownership.  Output arrays
+ *     are owned by the caller (host or device memory, see dpg_expand_opts).
+ *   - Precision: DPG_FP32 computes rollouts and separating-axis tests in
+ *     FP32 and recomputes in FP64, on the GPU, every pair whose gap or
+ *     bounds margin lies within contact_band of zero and every ball test
+ *     within ball_band of the radius; DPG_FP64 computes everything in FP64.
+ */
+#ifndef DPG_H
+#define DPG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DPG_ABI_VERSION 1
+
+/* error codes */
+#define DPG_OK 0
+#define DPG_ERR_ARG -1      /* invalid argument */
+#define DPG_ERR_OOM -2      /* device or host allocation failed */
+#define DPG_ERR_CUDA -3     /* CUDA runtime error (see dpg_last_error) */
+#define DPG_ERR_TIMEOUT -4  /* a bounded device wait gave up */
+#define DPG_ERR_ABORTED -5  /* dpg_set_abort was raised */
+#define DPG_ERR_CAPACITY -6 /* output capacity too small; n_pairs holds the need */
+#define DPG_ERR_STATE -7    /* call order (e.g. expand before upload) */
+#define DPG_ERR_NODEVICE -8 /* no CUDA device / kernel image not loadable */
+
+/* robot kinds (the dynobench model names) */
+#define DPG_ROBOT_UNICYCLE1 0 /* unicycle1_v0: (x,y,theta), (v,w) */
+#define DPG_ROBOT_CAR1 1      /* car1_v0: (x,y,theta0,theta1), (v,phi) */
+#define DPG_ROBOT_QUAD3D 2    /* quadrotor_v0: (p, q xyzw, v, w), 4 thrusts */
+#define DPG_ROBOT_QUAD2D 3    /* quad2d_v0: (x,y,theta,vx,vy,w), 2 thrusts */
+
+/* verdicts (per checked pair) */
+#define DPG_VALID 0
+#define DPG_COLLISION 1
+#define DPG_OUT_OF_BOUNDS 2
+
+/* precision */
+#define DPG_FP32 0
+#define DPG_FP64 1
+
+/* per-pair flags */
+#define DPG_FLAG_CONTACT_RECHECK 1 /* verdict recomputed in FP64 (contact/bounds band) */
+
+/* Robot description: the subset of dynobench::Model_robot the expansion uses
+ * (nx, nu, ref_dt, distance_weights, collision geometry, dynamics
+ * constants).  dpg_robot_default fills the values of each model. */
+typedef struct dpg_robot_desc {
+  int32_t kind;
+  int32_t nx, nu;
+  int32_t n_parts;    /* collision parts (car1: car + trailer) */
+  double dt;          /* ref_dt */
+  double w[4];        /* distance_weights, one per metric block */
+  double box[2];      /* planar robots: box length (heading axis), width */
+  double hitch;       /* car1: car centre to trailer centre */
+  double wheelbase;   /* car1 */
+  double radius;      /* quad3d: collision sphere radius */
+  double mass;        /* quad3d */
+  double arm;         /* quad3d: motor arm length */
+  double t2t;         /* quad3d: thrust-to-torque ratio */
+  double inertia[3];  /* quad3d: diagonal inertia */
+  double ang_gain;    /* quad2d: m*l/I */
+  double g;           /* gravity */
+} dpg_robot_desc;
+
+typedef struct dpg_expand_opts {
+  double radius;          /* ball radius = alpha * delta (dbastar.cpp:585-586) */
+  int32_t precision;      /* DPG_FP32 or DPG_FP64 */
+  int32_t x_on_device;    /* x is a device pointer */
+  int32_t out_on_device;  /* output arrays are device pointers */
+  int32_t reserved;
+  double contact_band;    /* FP64 re-check band for gaps and bounds (1e-4) */
+  double ball_band;       /* FP64 re-check band around the radius (1e-5) */
+} dpg_expand_opts;
+
+/* Results, one row per in-ball (node, primitive) pair.  Rows are grouped by
+ * primitive, primitives in order of decreasing length, nodes ascending
+ * within a primitive.  Any array pointer may be NULL to skip that output. */
+typedef struct dpg_expand_out {
+  int64_t capacity;        /* in: rows available in the arrays below */
+  int64_t n_pairs;         /* out: rows produced (or needed, on DPG_ERR_CAPACITY) */
+  uint32_t *node;          /* node index */
+  uint32_t *prim;          /* primitive index (upload order = Motion::idx) */
+  uint8_t *verdict;        /* DPG_VALID / DPG_COLLISION / DPG_OUT_OF_BOUNDS */
+  int16_t *first_invalid;  /* first out-of-bounds or colliding state, or L */
+  void *end_state;         /* n_pairs x nx, float (DPG_FP32) or double (DPG_FP64) */
+  float *min_gap;          /* min axis-aligned clearance along the checked states */
+  uint8_t *flags;          /* DPG_FLAG_* */
+  /* counters (out) */
+  int64_t n_scanned;       /* node x primitive ball tests */
+  int64_t n_contact_recheck;
+  int64_t n_ball_recheck;
+} dpg_expand_out;
+
+typedef struct dpg_ctx dpg_ctx;
+
+/* version of this header the library was built with */
+int dpg_abi_version(void);
+const char *dpg_errstr(int code);
+
+/* fills the model constants of `kind` (returns DPG_ERR_ARG for an unknown kind) */
+int dpg_robot_default(int32_t kind, dpg_robot_desc *out);
+
+/* Create a context on `device` for the robot.  Replaces robot_factory plus
+ * the Expander constructor (dbastar.cpp:532-535, 585-586). */
+int dpg_create(dpg_ctx **ctx, int device, const dpg_robot_desc *robot);
+void dpg_destroy(dpg_ctx *ctx);
+const char *dpg_last_error(const dpg_ctx *ctx);
+
+/* Upload the primitive set: P motions, motion p has len[p] states (rows of
+ * nx doubles, concatenated) and len[p]-1 actions (rows of nu doubles).  The
+ * index p is Motion::idx.  Replaces load_motion_primitives_new's tables and
+ * the T_m tree build (src/ompl/robots.cpp:3061-3174, dbastar.cpp:564-575);
+ * the noise and quaternion normalisation of the loader are the caller's. */
+int dpg_upload_primitives(dpg_ctx *ctx, int32_t P, const int32_t *len,
+                          const double *states, const double *actions);
+
+/* Upload the environment: state position bounds (dim values each) and
+ * n_obs axis-aligned boxes (n_obs x dim corners).  Replaces load_env and the
+ * environment broadphase (dbastar.cpp:535). */
+int dpg_upload_env(dpg_ctx *ctx, int32_t dim, const double *lo, const double *hi,
+                   int32_t n_obs, const double *obs_lo, const double *obs_hi);
+
+/* Expand N frontier states (N x nx doubles).  Returns DPG_ERR_CAPACITY with
+ * out->n_pairs set when out->capacity is too small. */
+int dpg_expand(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x,
+               dpg_expand_out *out);
+
+/* Wait for the context's stream. */
+int dpg_sync(dpg_ctx *ctx);
+/* Raise (1) or clear (0) the abort flag polled by the device work queue. */
+int dpg_set_abort(dpg_ctx *ctx, int32_t flag);
+
+/* Page-locked host buffers (cudaHostAlloc) for inputs and outputs of
+ * dpg_expand, so the host<->device copies run at full link speed.  No
+ * counterpart in the reference (its expansion never leaves the host). */
+void *dpg_host_alloc(size_t bytes);
+void dpg_host_free(void *p);
+
+/* Device time of the last dpg_expand, split by stage (milliseconds):
+ * t[0] ball scan + compaction, t[1] exact check, t[2] FP64 re-check,
+ * t[3] host<->device copies.  Returns the number of stages written. */
+int dpg_last_timings(const dpg_ctx *ctx, double *t, int32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

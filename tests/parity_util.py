@@ -1,0 +1,53 @@
+"""Comparison of GPU expansion results against the oracle.
+
+Bars (the tolerances every parity test states):
+  pairs, verdicts, first_invalid   identical
+  end states                      FP64 path: 1e-9 absolute; FP32 path:
+                                  1e-5 relative (|d| <= 1e-5 * max(1, |x|));
+                                  wrapped angles compared modulo 2 pi
+  min_gap (FP32 output)           FP64 path: 1e-5; FP32 path: 2e-4 absolute
+"""
+import math
+
+import numpy as np
+
+from dynoplan_gb300 import workloads as W
+
+ANGLE_COMPS = {W.UNICYCLE1: [2], W.CAR1: [2, 3], W.QUAD2D: [2], W.QUAD3D: []}
+
+
+def sort_by_pair(res):
+    key = res["node"].astype(np.int64) * (1 << 32) + res["prim"].astype(np.int64)
+    order = np.argsort(key, kind="stable")
+    return {k: (v[order] if isinstance(v, np.ndarray) and v.shape[:1] == order.shape else v)
+            for k, v in res.items()}
+
+
+def compare(kind, gpu, ora, precision, min_gap=True):
+    """Assert parity; returns a dict of residuals for reporting."""
+    g = sort_by_pair(gpu)
+    o = sort_by_pair(ora)
+    assert g["n_pairs"] == o["n_pairs"], (g["n_pairs"], o["n_pairs"])
+    np.testing.assert_array_equal(g["node"], o["node"])
+    np.testing.assert_array_equal(g["prim"], o["prim"])
+    np.testing.assert_array_equal(g["verdict"], o["verdict"])
+    np.testing.assert_array_equal(g["first_invalid"], o["first_invalid"])
+    ge = g["end_state"].astype(np.float64)
+    oe = o["end_state"]
+    d = ge - oe
+    for c in ANGLE_COMPS[kind]:
+        d[:, c] = (d[:, c] + math.pi) % (2 * math.pi) - math.pi
+    if precision == 1:
+        tol = np.full_like(oe, 1e-9)
+    else:
+        tol = 1e-5 * np.maximum(1.0, np.abs(oe))
+    bad = np.abs(d) > tol
+    assert not bad.any(), f"end state mismatch at {np.argwhere(bad)[:5].tolist()}: max {np.abs(d).max()}"
+    out = {"end_state_max_abs": float(np.abs(d).max()) if len(d) else 0.0}
+    if min_gap and len(d):
+        fin = np.isfinite(o["min_gap"])
+        np.testing.assert_array_equal(np.isfinite(g["min_gap"]), fin)
+        gm = np.abs(g["min_gap"][fin].astype(np.float64) - o["min_gap"][fin])
+        assert gm.max(initial=0) <= (1e-5 if precision == 1 else 2e-4), gm.max(initial=0)
+        out["min_gap_max_abs"] = float(gm.max(initial=0))
+    return out

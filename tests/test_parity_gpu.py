@@ -1,0 +1,199 @@
+"""GPU expansion vs the FP64 oracle, through the C ABI (needs a GB300).
+
+Bars: identical neighbour pairs, verdicts and first-invalid states; end
+states within 1e-9 (FP64 path) or 1e-5 relative (FP32 path); see
+tests/parity_util.py.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_bind as ob
+from dynoplan_gb300 import workloads as W
+from parity_util import compare
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def gpu(dpg_lib):
+    from dynoplan_gb300 import gpu as G
+    return G
+
+
+def run_gpu(G, wl, precision, **kw):
+    with G.Context(wl.robot) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        return ctx.expand(wl.nodes, wl.radius, precision=precision, **kw)
+
+
+@pytest.mark.parametrize("cfg", [1, 2, 3, 5])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_golden_fixture(gpu, cfg, precision):
+    """The committed oracle outputs (tests/golden/oracle_cfg*.npz)."""
+    z = np.load(os.path.join(GOLD, f"oracle_cfg{cfg}.npz"))
+    kind = int(z["kind"])
+    wl = W.Workload("golden", W.robot_model(kind), W.Primitives(z["length"], z["states"], z["actions"]),
+                    W.Env(z["env_lo"], z["env_hi"], z["obs_lo"], z["obs_hi"]), z["nodes"],
+                    delta=2.0 * float(z["radius"]), alpha=0.5, precision=precision, seed=0)
+    res = run_gpu(gpu, wl, precision)
+    ora = {k: z[k] for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap")}
+    ora["n_pairs"] = len(z["node"])
+    compare(kind, res, ora, precision)
+
+
+@pytest.mark.parametrize("cfg,scale", [(1, 0.1), (2, 0.02), (3, 0.01), (5, 0.01)])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_parity_seeded(gpu, cfg, scale, precision):
+    wl = W.make_workload(cfg, scale=scale, seed=77 + cfg)
+    res = run_gpu(gpu, wl, precision)
+    ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius, fast=True,
+                    threads=ob.lib().orc_max_threads())
+    assert ora["n_pairs"] > 0
+    # the fast baseline carries no min_gap; compare that on the plain oracle below
+    compare(wl.robot.kind, res, ora, precision, min_gap=False)
+
+
+@pytest.mark.parametrize("cfg", [1, 2, 3, 5])
+def test_min_gap_and_flags(gpu, cfg):
+    wl = W.make_workload(cfg, scale=0.005 if cfg != 1 else 0.03, seed=5 + cfg)
+    res = run_gpu(gpu, wl, 0)
+    ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius)
+    compare(wl.robot.kind, res, ora, 0)
+    assert set(np.unique(res["flags"])) <= {0, 1}
+
+
+def exact_start_primitives(m, P, steps, seed):
+    """Primitives starting exactly at the canonical zero state (no loader
+    noise), so the first transformed state is the node's position with
+    heading 0."""
+    rng = W.Rng(seed)
+    lb, ub = np.array(m.u_lb), np.array(m.u_ub)
+    states, actions, length = [], [], []
+    for p in range(P):
+        U = lb + (ub - lb) * rng.uniform((steps, m.nu))
+        X = [np.zeros(m.nx)]
+        for k in range(steps):
+            X.append(W.step(m, X[-1][None], U[k][None])[0])
+        states.append(np.array(X))
+        actions.append(U)
+        length.append(steps + 1)
+    return W.Primitives(np.array(length, np.int32), np.concatenate(states), np.concatenate(actions))
+
+
+@pytest.mark.parametrize("kind", [W.UNICYCLE1, W.CAR1, W.QUAD2D])
+def test_contact_band_recheck(gpu, kind):
+    """Nodes placed so the robot box touches an obstacle face at the first
+    state (gap exactly 0, or within 1e-7 / 3e-5 of it): the FP32 gap falls in
+    the band, the pair is recomputed in FP64, and every verdict equals the
+    oracle's."""
+    m = W.robot_model(kind)
+    prims = exact_start_primitives(m, 32, 12, seed=11)
+    env = W.Env(np.zeros(2), np.array([8.0, 8.0]), np.array([[4.0, 1.0]]), np.array([[5.0, 7.0]]))
+    xs = []
+    for dx in (0.0, 1e-7, -1e-7, 3e-5, -3e-5):
+        x = np.zeros(m.nx)
+        x[0], x[1] = 4.0 - 0.25 + dx, 4.0   # box half length 0.25 along heading 0
+        xs.append(x)
+    nodes = np.array(xs)
+    with gpu.Context(m) as ctx:
+        ctx.upload_primitives(prims)
+        ctx.upload_env(env)
+        res = ctx.expand(nodes, 100.0, precision=0)
+    ora = ob.expand(m, prims, env, nodes, 100.0)
+    assert ora["n_pairs"] == 5 * 32
+    compare(kind, res, ora, 0)
+    assert res["n_contact_recheck"] >= 3 * 32
+    assert (res["flags"] == 1).sum() == res["n_contact_recheck"]
+    assert (res["verdict"][res["node"] == 0] == 1).all()   # touching is contact
+
+
+def test_edge_cases(gpu):
+    m = W.robot_model(W.UNICYCLE1)
+    prims = W.make_primitives(m, 40, 0, 12, seed=21)   # some single-state motions
+    assert prims.length.min() == 1
+    env = W.make_env((6.0, 6.0), 10, 0.2, 1.0, seed=22)
+    nodes = W.make_nodes(m, env, 300, seed=23)
+    with gpu.Context(m) as ctx:
+        ctx.upload_primitives(prims)
+        ctx.upload_env(env)
+        # no nodes
+        assert ctx.expand(nodes[:0], 0.15)["n_pairs"] == 0
+        # radius 0: nothing in the ball (starts carry 1e-7 noise)
+        assert ctx.expand(nodes, 0.0)["n_pairs"] == 0
+        # every pair in the ball
+        res = ctx.expand(nodes, 100.0, precision=1)
+        assert res["n_pairs"] == 300 * 40
+        compare(W.UNICYCLE1, res, ob.expand(m, prims, env, nodes, 100.0), 1)
+        # capacity too small: error with the needed count, then retry
+        from dynoplan_gb300 import _lib
+        with pytest.raises(_lib.DpgError) as e:
+            ctx.expand(nodes, 100.0, outputs=dict(
+                node=np.empty(10, np.uint32), prim=np.empty(10, np.uint32), verdict=np.empty(10, np.uint8),
+                first_invalid=np.empty(10, np.int16), end_state=np.empty((10, 3), np.float32),
+                min_gap=np.empty(10, np.float32), flags=np.empty(10, np.uint8)), capacity=10)
+        assert e.value.code == _lib.DPG_ERR_CAPACITY
+        # abort flag
+        ctx.set_abort(True)
+        with pytest.raises(_lib.DpgError) as e:
+            ctx.expand(nodes, 0.15)
+        assert e.value.code == _lib.DPG_ERR_ABORTED
+        ctx.set_abort(False)
+        assert ctx.expand(nodes, 0.15)["n_pairs"] > 0
+    # empty environment: collisions impossible
+    env0 = W.Env(np.zeros(2), np.array([6.0, 6.0]), np.zeros((0, 2)), np.zeros((0, 2)))
+    with gpu.Context(m) as ctx:
+        ctx.upload_primitives(prims)
+        ctx.upload_env(env0)
+        res = ctx.expand(nodes, 0.15)
+        assert DPG_COLLISION_free(res)
+        compare(W.UNICYCLE1, res, ob.expand(m, prims, env0, nodes, 0.15), 0)
+
+
+def DPG_COLLISION_free(res):
+    return not (res["verdict"] == 1).any()
+
+
+def test_bad_arguments(gpu):
+    from dynoplan_gb300 import _lib
+    m = W.robot_model(W.CAR1)
+    with gpu.Context(m) as ctx:
+        with pytest.raises(_lib.DpgError) as e:   # expand before upload
+            ctx.expand(np.zeros((4, 4)), 0.15)
+        assert e.value.code == _lib.DPG_ERR_STATE
+        with pytest.raises(_lib.DpgError):        # wrong env dimension
+            ctx.upload_env(W.Env(np.zeros(3), np.ones(3), np.zeros((0, 3)), np.zeros((0, 3))))
+
+
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_full_size_parity(gpu, cfg):
+    """The full workload (config sizes), every pair against the multi-threaded
+    oracle: identical pairs and verdicts, end states within tolerance."""
+    wl = W.make_workload(cfg)
+    res = run_gpu(gpu, wl, wl.precision)
+    ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius, fast=True,
+                    threads=ob.lib().orc_max_threads())
+    compare(wl.robot.kind, res, ora, wl.precision, min_gap=False)
+
+
+def test_full_size_quadrotor_subset_and_determinism(gpu):
+    """quadrotor_v0 at full size: two runs agree bit for bit; the pairs of a
+    node subset agree with the oracle."""
+    wl = W.make_workload(3)
+    with gpu.Context(wl.robot) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        a = ctx.expand(wl.nodes, wl.radius, precision=0)
+        b = ctx.expand(wl.nodes, wl.radius, precision=0)
+        for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap", "flags"):
+            np.testing.assert_array_equal(a[k], b[k])
+        sub = wl.nodes[:1500]
+        s = ctx.expand(sub, wl.radius, precision=0)
+    ora = ob.expand(wl.robot, wl.prims, wl.env, sub, wl.radius, fast=True, threads=ob.lib().orc_max_threads())
+    compare(wl.robot.kind, s, ora, 0, min_gap=False)
+    sel = a["node"] < 1500
+    assert sel.sum() == s["n_pairs"]
