@@ -444,7 +444,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
 
   bool done = !active, collided = false;
   int first_oob = L, first_col = L, amb = 0;
-  Real mg = Real(1e30);
+  Real mg = Real(INFINITY);  // no obstacle: +inf
   const Real hl = Real(rp.half_len), hw = Real(rp.half_wid), rad = Real(rp.radius);
 
   for (int k = 0; k < L; k++) {

@@ -419,7 +419,7 @@ int orc_check_pair(const orc_robot *r, const orc_env *e, const orc_prims *pr,
   }
   memcpy(end_state, xs + (size_t)(L - 1) * nx, sizeof(double) * (size_t)nx);
   /* is_motion_collision_free over every state (dbastar.cpp:461-485) */
-  double mg = 1e300;
+  double mg = INFINITY; /* no obstacle: +inf */
   for (int s = 0; s < L; s++) {
     const double *x = xs + (size_t)s * nx;
     part_pose pp[2];
