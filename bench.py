@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "checked (node,primitive) expansions/s"
 UNIT = "pairs/s"
-KERNELS_PER_STEP = 7  # prep_nodes nn_mask nn_prefix scan_totals nn_emit check_pairs recheck_pairs
+KERNELS_PER_STEP = 6  # prep_nodes nn_mask nn_prefix scan_totals nn_emit check_pairs
 L2_FLUSH_BYTES = 512 << 20
 
 # DRAM bytes per check_pairs launch from ncu (dram__bytes_read.sum +
@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--nodes", type=int, default=None, help="frontier states per step (default: the workload's)")
     return ap.parse_args()
 
 
@@ -205,7 +207,7 @@ def run_ours(args, rank, world, local_rank):
     # weak scaling: every rank expands its own frontier batch (replicas; the
     # nodes are independent, no exchange)
     c = W.CONFIGS[args.config]
-    wl = W.make_workload(args.config)
+    wl = W.make_workload(args.config, N=args.nodes)
     if rank > 0:
         wl.nodes = W.make_nodes(wl.robot, wl.env, len(wl.nodes), seed=wl.seed + 13 + 1000 * rank)
     N, nx = wl.nodes.shape
@@ -238,7 +240,7 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         torch.distributed.barrier()
     clocks = Clocks(dev)
-    dev_ms, check_ms, pairs_total, rechecks = [], [], 0, 0
+    dev_ms, check_ms, stage, pairs_total, rechecks = [], [], [], 0, 0
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
         lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
@@ -246,6 +248,7 @@ def run_ours(args, rank, world, local_rank):
         t = ctx.timings()
         dev_ms.append(sum(t[:4]))
         check_ms.append(t[1])
+        stage.append(t)
         pairs_total += r["n_pairs"]
         rechecks += r["n_contact_recheck"]
     torch.cuda.synchronize()
@@ -271,27 +274,9 @@ def run_ours(args, rank, world, local_rank):
     achieved = alg_ops / check_s / 1e12
 
     # ---------------- e2e through the C ABI with host buffers
-    xh = G.PinnedArray(wl.nodes.shape, np.float64)
-    xh.array[:] = wl.nodes
-    hosts = {
-        "node": G.PinnedArray(cap, np.uint32), "prim": G.PinnedArray(cap, np.uint32),
-        "verdict": G.PinnedArray(cap, np.uint8), "first_invalid": G.PinnedArray(cap, np.int16),
-        "end_state": G.PinnedArray((cap, nx), np.float64 if prec == 1 else np.float32),
-        "min_gap": G.PinnedArray(cap, np.float32), "flags": G.PinnedArray(cap, np.uint8),
-    }
-    host_out = {k: v.array for k, v in hosts.items()}
-    for _ in range(args.warmup):
-        ctx.expand(xh.array, wl.radius, precision=prec, capacity=cap, outputs=host_out)
-    e2e_s, e2e_pairs = 0.0, 0
-    for _ in range(args.steps):
-        lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
-        t0 = time.perf_counter()
-        r = ctx.expand(xh.array, wl.radius, precision=prec, capacity=cap, outputs=host_out)
-        e2e_s += time.perf_counter() - t0
-        e2e_pairs += r["n_pairs"]
-    d2h = n_pairs * (4 + 4 + 1 + 2 + es_bytes * nx + 4 + 1)
-    e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * nx * 8),
-           "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s / args.steps}
+    e2e, pinned = None, []
+    if not args.no_e2e:
+        e2e, pinned = run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -304,7 +289,7 @@ def run_ours(args, rank, world, local_rank):
                "sample": f"{n} of {N} frontier states ({cp} checked pairs, {dt:.1f} s)",
                "value_1_thread": rate1, "sample_1_thread": f"{n1} frontier states ({dt1:.1f} s)"}
 
-    for h in list(hosts.values()) + [xh]:
+    for h in pinned:
         h.free()
     ctx.close()
     if rank != 0:
@@ -328,11 +313,40 @@ def run_ours(args, rank, world, local_rank):
                      "peak_source": "FMA-chain kernel on this device (dpg_bench_fp32_peak); "
                                     "MEASURED_PEAKS.json holds HBM and bf16 only",
                      "alg_ops_per_launch": alg_ops, "check_ms": 1e3 * check_s},
-        "stage_ms": {"ball_scan": None, "check": 1e3 * check_s},
+        "stage_ms": {k: statistics.mean(t[i] for t in stage) for i, k in
+                     enumerate(("ball_scan", "check", "fp64_recheck", "copies"))},
         "cpu_baseline": cpu,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
+
+
+def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
+    """The C ABI with page-locked host buffers: H2D of the nodes, the expand,
+    D2H of every output; wall clock per call."""
+    N, nx = wl.nodes.shape
+    xh = G.PinnedArray(wl.nodes.shape, np.float64)
+    xh.array[:] = wl.nodes
+    hosts = {
+        "node": G.PinnedArray(cap, np.uint32), "prim": G.PinnedArray(cap, np.uint32),
+        "verdict": G.PinnedArray(cap, np.uint8), "first_invalid": G.PinnedArray(cap, np.int16),
+        "end_state": G.PinnedArray((cap, nx), np.float64 if prec == 1 else np.float32),
+        "min_gap": G.PinnedArray(cap, np.float32), "flags": G.PinnedArray(cap, np.uint8),
+    }
+    host_out = {k: v.array for k, v in hosts.items()}
+    for _ in range(args.warmup):
+        ctx.expand(xh.array, wl.radius, precision=prec, capacity=cap, outputs=host_out)
+    e2e_s, e2e_pairs = 0.0, 0
+    for _ in range(args.steps):
+        lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
+        t0 = time.perf_counter()
+        r = ctx.expand(xh.array, wl.radius, precision=prec, capacity=cap, outputs=host_out)
+        e2e_s += time.perf_counter() - t0
+        e2e_pairs += r["n_pairs"]
+    d2h = n_pairs * (4 + 4 + 1 + 2 + es_bytes * nx + 4 + 1)
+    e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * nx * 8),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s / args.steps}
+    return e2e, list(hosts.values()) + [xh]
 
 
 def ctypes_peak(lib, dev):

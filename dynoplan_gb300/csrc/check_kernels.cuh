@@ -1,0 +1,424 @@
+// check_kernels.cuh -- exact checking of (primitive, node) pairs on sm_103a.
+//
+// Replaces LazyTraj::compute + check_lazy_trajectory
+// (include/dynoplan/dbastar/dbastar.hpp:166-230, src/dbastar/dbastar.cpp:391-490)
+// for every in-ball pair of a batch.
+//
+// Work decomposition: persistent warps take (primitive, 32 nodes) items from a
+// device counter, longest primitives first.  The 32 lanes walk the same
+// primitive in lockstep, so the per-state pose rows are warp-broadcast loads
+// and the lanes differ only by their node offset.
+//
+// Transform: position_k = canonical_k + p0 (+ k*dt*v0), velocity_k =
+// canonical_k + v0, other components canonical_k.  That is the translation of
+// the stored states (unicycle1, car1) and, exactly, the re-rollout from the
+// shifted start for quad2d / quadrotor (no dynamics term depends on position
+// or velocity); the canonical rollout is FP64, once per upload.
+//
+// Obstacles (shared memory) are culled per lane in two levels, both with a
+// margin of kGapCap + band + slack so nothing that could touch the robot,
+// fall in the FP64 band or set min_gap is dropped:
+//   1. against the bounding box of the whole transformed primitive (once per
+//      pair; bitmask over <= kMaxCullObs obstacles),
+//   2. against the box of each chunk of kChunk states (from the level-1 set),
+// then every state tests its chunk's candidates (separating axes, AABB early
+// reject).  A test whose FP32 gap lies within `band` of zero, and a bounds
+// test within `band` of a bound, is recomputed in FP64 from the FP64 tables
+// on the spot, so verdicts equal the FP64 oracle's.
+#pragma once
+
+#include "expand_kernels.cuh"
+
+namespace dpg {
+
+struct CheckArgs {
+  RobotParams rp;
+  PrimView pv;
+  NodeView nv;
+  EnvView ev;
+  PairView out;
+  const unsigned long long *ord_pbase;
+  const unsigned long long *ord_ibase;
+  DevCounters *ctr;
+  const volatile int *abort_flag;
+  double band;       // FP64 re-check band (0 on the FP64 path)
+  float cull_margin; // obstacle culling margin
+};
+
+template <class Real> __device__ __forceinline__ const Pose<Real> *pose_table(const PrimView &pv);
+template <> __device__ __forceinline__ const Pose<float> *pose_table<float>(const PrimView &pv) { return pv.pose32; }
+template <> __device__ __forceinline__ const Pose<double> *pose_table<double>(const PrimView &pv) { return pv.pose64; }
+
+// node offset component i (position i < POSD, then velocity)
+template <class Real> __device__ __forceinline__ Real node_off(const NodeView &nv, int64_t n, int i, int nx, int comp);
+template <> __device__ __forceinline__ float node_off<float>(const NodeView &nv, int64_t n, int i, int nx, int comp) {
+  return nv.off32[i * nv.N + n];
+}
+template <> __device__ __forceinline__ double node_off<double>(const NodeView &nv, int64_t n, int i, int nx, int comp) {
+  return nv.x64[n * nx + comp];
+}
+
+// ------------------------------------------------------------ narrow phase --
+
+// Oriented box (pose c,s; half extents a,b; axis-aligned half extents ex,ey)
+// against an obstacle box.  Returns 0 clear, 1 contact, 2 ambiguous (|gap| <=
+// band, FP32 path).  mg takes the axis-aligned clearance.
+template <class Real, bool BAND>
+__device__ __forceinline__ int planar_test(Real px, Real py, Real c, Real s, Real ex, Real ey,
+                                           const Obs2<Real> &ob, Real a, Real b, Real band, Real &mg) {
+  const Real dx = px - ob.cx, dy = py - ob.cy;
+  const Real g = fmax(fabs(dx) - (ex + ob.hx), fabs(dy) - (ey + ob.hy));
+  mg = fmin(mg, g);
+  if (g > band) return 0;
+  const Real ac = fabs(c), as = fabs(s);
+  const Real du = dx * c + dy * s, dv = dy * c - dx * s;
+  const Real gu = fabs(du) - (a + ob.hx * ac + ob.hy * as);
+  const Real gv = fabs(dv) - (b + ob.hx * as + ob.hy * ac);
+  const Real gs = fmax(g, fmax(gu, gv));
+  if (BAND) {
+    if (gs > band) return 0;
+    return gs < -band ? 1 : 2;
+  }
+  return gs <= Real(0) ? 1 : 0;
+}
+
+template <class Real, bool BAND>
+__device__ __forceinline__ int sphere_test(Real px, Real py, Real pz, const Obs3<Real> &ob, Real rad,
+                                           Real band, Real &mg) {
+  const Real dx = fabs(px - ob.cx) - ob.hx, dy = fabs(py - ob.cy) - ob.hy, dz = fabs(pz - ob.cz) - ob.hz;
+  const Real m = fmax(dx, fmax(dy, dz));
+  const Real g = m - rad;
+  mg = fmin(mg, g);
+  if (g > band) return 0;
+  const Real ux = fmax(dx, Real(0)), uy = fmax(dy, Real(0)), uz = fmax(dz, Real(0));
+  const Real gs = (m <= Real(0) ? m : sqrt(ux * ux + uy * uy + uz * uz)) - rad;
+  if (BAND) {
+    if (gs > band) return 0;
+    return gs < -band ? 1 : 2;
+  }
+  return gs <= Real(0) ? 1 : 0;
+}
+
+// FP64 position component i of state k (affine transform of the FP64 table)
+template <int KIND>
+__device__ __forceinline__ double pos64(const CheckArgs &A, int64_t row, int k, const double *x64, int i) {
+  using R = Robot<KIND>;
+  const Pose<double> ps = A.pv.pose64[row];  // part 0 = the state position
+  double v = (i == 0 ? ps.cx : (i == 1 ? ps.cy : ps.c)) + x64[i];
+  if (R::VELOFF) v += (double(k) * A.rp.dt) * x64[R::vel_comp(i)];
+  return v;
+}
+
+// FP64 separating-axis gap of part q at state k against obstacle o (the
+// oracle's formula, from the FP64 tables).
+template <int KIND>
+__device__ double gap64(const CheckArgs &A, int64_t s0, int k, int q, const double *x64, int o) {
+  using R = Robot<KIND>;
+  const RobotParams &rp = A.rp;
+  double sx = x64[0], sy = x64[1], sz = R::POSD == 3 ? x64[2] : 0.0;
+  if (R::VELOFF) {
+    const double t = double(k) * rp.dt;
+    sx += t * x64[R::vel_comp(0)];
+    sy += t * x64[R::vel_comp(1)];
+    if (R::POSD == 3) sz += t * x64[R::vel_comp(2)];
+  }
+  const Pose<double> ps = A.pv.pose64[q * A.pv.S + s0 + k];
+  if constexpr (R::SPHERE) {
+    const Obs3<double> ob = ((const Obs3<double> *)A.ev.obs64)[o];
+    const double dx = fabs(ps.cx + sx - ob.cx) - ob.hx, dy = fabs(ps.cy + sy - ob.cy) - ob.hy,
+                 dz = fabs(ps.c + sz - ob.cz) - ob.hz;
+    const double m = fmax(dx, fmax(dy, dz));
+    const double ux = fmax(dx, 0.0), uy = fmax(dy, 0.0), uz = fmax(dz, 0.0);
+    return (m <= 0 ? m : sqrt(ux * ux + uy * uy + uz * uz)) - rp.radius;
+  } else {
+    const Obs2<double> ob = ((const Obs2<double> *)A.ev.obs64)[o];
+    const double px = ps.cx + sx, py = ps.cy + sy;
+    const double ac = fabs(ps.c), as = fabs(ps.s);
+    const double a = rp.half_len, b = rp.half_wid;
+    const double dx = px - ob.cx, dy = py - ob.cy;
+    const double gx = fabs(dx) - (a * ac + b * as + ob.hx);
+    const double gy = fabs(dy) - (a * as + b * ac + ob.hy);
+    const double du = dx * ps.c + dy * ps.s, dv = -dx * ps.s + dy * ps.c;
+    const double gu = fabs(du) - (a + ob.hx * ac + ob.hy * as);
+    const double gv = fabs(dv) - (b + ob.hx * as + ob.hy * ac);
+    return fmax(fmax(gx, gy), fmax(gu, gv));
+  }
+}
+
+// box (centre cen, half hf) against obstacle box, with margin
+template <int D, class Real>
+__device__ __forceinline__ bool near_box(const float *cen, const float *hf, const void *obs_sm, int o, float M) {
+  if constexpr (D == 2) {
+    const Obs2<Real> ob = ((const Obs2<Real> *)obs_sm)[o];
+    return fabsf(cen[0] - (float)ob.cx) <= hf[0] + (float)ob.hx + M &&
+           fabsf(cen[1] - (float)ob.cy) <= hf[1] + (float)ob.hy + M;
+  } else {
+    const Obs3<Real> ob = ((const Obs3<Real> *)obs_sm)[o];
+    return fabsf(cen[0] - (float)ob.cx) <= hf[0] + (float)ob.hx + M &&
+           fabsf(cen[1] - (float)ob.cy) <= hf[1] + (float)ob.hy + M &&
+           fabsf(cen[2] - (float)ob.cz) <= hf[2] + (float)ob.hz + M;
+  }
+}
+
+// ------------------------------------------------------------- one pair ----
+
+template <int KIND, class Real, bool BAND, bool CULL, bool LOCKSTEP>
+__device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t pair, uint32_t node,
+                          bool active) {
+  using R = Robot<KIND>;
+  constexpr int D = R::POSD, V = R::VELOFF;
+  const PrimView &pv = A.pv;
+  const RobotParams &rp = A.rp;
+  const int L = pv.len[p];
+  const int64_t s0 = pv.soff[p];
+  const Pose<Real> *pose = pose_table<Real>(pv);
+  const Real band = BAND ? Real(A.band) : Real(0);
+  const double *x64 = A.nv.x64 + (int64_t)(active ? node : 0) * R::NX;
+  const int n_obs = A.ev.n_obs;
+
+  Real off[D + V];
+#pragma unroll
+  for (int i = 0; i < D; i++) off[i] = active ? node_off<Real>(A.nv, node, i, R::NX, i) : Real(0);
+#pragma unroll
+  for (int i = 0; i < V; i++) off[D + i] = active ? node_off<Real>(A.nv, node, D + i, R::NX, R::vel_comp(i)) : Real(0);
+
+  // bounds pre-check on the swept box of the positions (FP64)
+  bool need_bounds = true;
+  if (active) {
+    const double *bx = pv.pbox + (int64_t)p * 2 * D;
+    const double tmax = (L - 1) * rp.dt;
+    bool inside = true;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      double lo = bx[i] + x64[i], hi = bx[D + i] + x64[i];
+      if (V) {
+        const double sv = tmax * x64[R::vel_comp(i)];
+        lo += fmin(sv, 0.0);
+        hi += fmax(sv, 0.0);
+      }
+      inside = inside && lo > A.ev.lo[i] + A.band && hi < A.ev.hi[i] - A.band;
+    }
+    need_bounds = !inside;
+  }
+
+  // level-1 culling: obstacles near the whole transformed primitive
+  uint32_t l1[kMaxCullObs / 32] = {0u, 0u, 0u, 0u};
+  const float M = A.cull_margin;
+  if (CULL && active) {
+    const float *tb = pv.tbox32 + (int64_t)p * 2 * D;
+    const float tmax = float(L - 1) * float(rp.dt);
+    float cen[D], hf[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      cen[i] = tb[i] + (float)off[i];
+      hf[i] = tb[D + i];
+      if (V) {
+        const float sv = tmax * (float)off[D + i];
+        cen[i] += 0.5f * sv;
+        hf[i] += 0.5f * fabsf(sv);
+      }
+    }
+    for (int o = 0; o < n_obs; o++)
+      if (near_box<D, Real>(cen, hf, obs_sm, o, M)) l1[o >> 5] |= 1u << (o & 31);
+  }
+
+  bool done = !active, collided = false, rechecked = false;
+  int first_oob = L, first_col = L;
+  Real mg = Real(INFINITY);
+  const Real hl = Real(rp.half_len), hw = Real(rp.half_wid), rad = Real(rp.radius);
+  uint32_t cm[kMaxCullObs / 32] = {0u, 0u, 0u, 0u};
+
+  for (int k = 0; k < L; k++) {
+    if (LOCKSTEP) {
+      if (!__any_sync(kFull, !done)) break;
+    } else if (done) {
+      break;
+    }
+    const Real t = Real(k) * Real(rp.dt);
+    // level-2 culling at each chunk start
+    if (CULL && (k % kChunk) == 0 && !done && !collided) {
+      const float *cb = pv.cbox32 + (pv.coff[p] + k / kChunk) * 2 * D;
+      const float t0 = float(k) * float(rp.dt), t1 = float(min(L - 1, k + kChunk - 1)) * float(rp.dt);
+      float cen[D], hf[D];
+#pragma unroll
+      for (int i = 0; i < D; i++) {
+        cen[i] = cb[i] + (float)off[i];
+        hf[i] = cb[D + i];
+        if (V) {
+          const float v = (float)off[D + i];
+          cen[i] += 0.5f * (t0 + t1) * v;
+          hf[i] += 0.5f * (t1 - t0) * fabsf(v);
+        }
+      }
+#pragma unroll
+      for (int w = 0; w < kMaxCullObs / 32; w++) {
+        uint32_t m = l1[w], c = 0;
+        while (m) {
+          const int b = __ffs(m) - 1;
+          m &= m - 1;
+          if (near_box<D, Real>(cen, hf, obs_sm, 32 * w + b, M)) c |= 1u << b;
+        }
+        cm[w] = c;
+      }
+    }
+    if (done) continue;
+    // per-state geometry (identical for the 32 lanes)
+    Pose<Real> ps[R::PARTS];
+#pragma unroll
+    for (int q = 0; q < R::PARTS; q++) ps[q] = pose[q * pv.S + s0 + k];
+    Real sx = off[0], sy = off[1], sz = Real(0);
+    if (V) { sx += t * off[D + 0]; sy += t * off[D + 1]; }
+    if (D == 3) { sz = off[2]; if (V) sz += t * off[D + 2]; }
+    if (need_bounds) {
+      const Real pv3[3] = {ps[0].cx + sx, ps[0].cy + sy, ps[0].c + sz};
+      int bt = 0;
+#pragma unroll
+      for (int i = 0; i < D; i++) {
+        int r;
+        if (BAND) {
+          const Real v = pv3[i];
+          const Real lo = Real(A.ev.lo[i]), hi = Real(A.ev.hi[i]);
+          r = (v < lo - band || v > hi + band) ? 1 : ((v <= lo + band || v >= hi - band) ? 2 : 0);
+          if (r == 2) {  // decide in FP64
+            const double v64 = pos64<KIND>(A, s0 + k, k, x64, i);
+            r = (v64 >= A.ev.lo[i] && v64 <= A.ev.hi[i]) ? 0 : 1;
+            rechecked = true;
+          }
+        } else {
+          r = (pv3[i] >= Real(A.ev.lo[i]) && pv3[i] <= Real(A.ev.hi[i])) ? 0 : 1;
+        }
+        bt |= r;
+      }
+      if (bt) { first_oob = k; done = true; continue; }
+    }
+    if (collided) continue;
+    bool hit = false;
+    auto test_obstacle = [&](int o) {
+      if constexpr (R::SPHERE) {
+        const Obs3<Real> ob = ((const Obs3<Real> *)obs_sm)[o];
+        int r = sphere_test<Real, BAND>(ps[0].cx + sx, ps[0].cy + sy, ps[0].c + sz, ob, rad, band, mg);
+        if (BAND && r == 2) { r = gap64<KIND>(A, s0, k, 0, x64, o) <= 0.0 ? 1 : 0; rechecked = true; }
+        hit |= r == 1;
+      } else {
+        const Obs2<Real> ob = ((const Obs2<Real> *)obs_sm)[o];
+#pragma unroll
+        for (int q = 0; q < R::PARTS; q++) {
+          const Real ac = fabs(ps[q].c), as = fabs(ps[q].s);
+          const Real ex = hl * ac + hw * as, ey = hl * as + hw * ac;
+          int r = planar_test<Real, BAND>(ps[q].cx + sx, ps[q].cy + sy, ps[q].c, ps[q].s, ex, ey, ob, hl, hw,
+                                          band, mg);
+          if (BAND && r == 2) { r = gap64<KIND>(A, s0, k, q, x64, o) <= 0.0 ? 1 : 0; rechecked = true; }
+          hit |= r == 1;
+        }
+      }
+    };
+    if (CULL) {
+#pragma unroll
+      for (int w = 0; w < kMaxCullObs / 32; w++) {
+        uint32_t m = cm[w];
+        while (m) {
+          const int b = __ffs(m) - 1;
+          m &= m - 1;
+          test_obstacle(32 * w + b);
+        }
+      }
+    } else {
+      for (int o = 0; o < n_obs; o++) test_obstacle(o);
+    }
+    if (hit) {
+      collided = true;
+      first_col = k;
+      if (!need_bounds) done = true;
+    }
+  }
+
+  const unsigned rmask = LOCKSTEP ? __ballot_sync(kFull, active && rechecked) : 0u;
+  if (LOCKSTEP && (threadIdx.x & 31) == 0 && rmask) atomicAdd(&A.ctr->n_recheck, (unsigned long long)__popc(rmask));
+  if (!active) return;
+  const PairView &o = A.out;
+  uint8_t verdict;
+  int fi;
+  if (first_oob < L) { verdict = DPG_OUT_OF_BOUNDS; fi = first_oob; }
+  else if (collided) { verdict = DPG_COLLISION; fi = first_col; }
+  else { verdict = DPG_VALID; fi = L; }
+  const int er = first_oob < L ? first_oob : L - 1;  // end-state row
+  if (o.verdict) o.verdict[pair] = verdict;
+  if (o.first_invalid) o.first_invalid[pair] = (int16_t)fi;
+  if (o.min_gap)
+    o.min_gap[pair] = verdict == DPG_OUT_OF_BOUNDS ? __int_as_float(0x7fc00000)
+                                                   : ((float)mg <= kGapCap ? (float)mg : __int_as_float(0x7f800000));
+  if (o.flags) o.flags[pair] = rechecked ? DPG_FLAG_CONTACT_RECHECK : 0;
+  if (o.end_state) {
+    Real *es = (Real *)o.end_state + pair * R::NX;
+    const Real t = Real(er) * Real(rp.dt);
+    const int64_t row = s0 + er;
+#pragma unroll
+    for (int c = 0; c < R::NX; c++) {
+      Real v = sizeof(Real) == 4 ? Real(pv.st32[row * R::NX + c]) : Real(pv.st64[row * R::NX + c]);
+      if (c < D) {
+        v += off[c];
+        if (V) v += t * off[D + c];
+      }
+#pragma unroll
+      for (int i = 0; i < V; i++)
+        if (c == R::vel_comp(i)) v += off[D + i];
+      es[c] = v;
+    }
+  }
+}
+
+template <class Real, int KIND>
+__device__ void load_obstacles(const EnvView &ev, void *sm) {
+  using R = Robot<KIND>;
+  if constexpr (R::SPHERE) {
+    const Obs3<Real> *src = (const Obs3<Real> *)(sizeof(Real) == 4 ? ev.obs32 : ev.obs64);
+    Obs3<Real> *dst = (Obs3<Real> *)sm;
+    for (int i = threadIdx.x; i < ev.n_obs; i += blockDim.x) dst[i] = src[i];
+  } else {
+    const Obs2<Real> *src = (const Obs2<Real> *)(sizeof(Real) == 4 ? ev.obs32 : ev.obs64);
+    Obs2<Real> *dst = (Obs2<Real> *)sm;
+    for (int i = threadIdx.x; i < ev.n_obs; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+}
+
+// Persistent warps over (primitive, 32 nodes) work items.
+template <int KIND, class Real, bool BAND, bool CULL>
+__global__ void __launch_bounds__(kCheckThreads) check_pairs(CheckArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  load_obstacles<Real, KIND>(A.ev, smem);
+  const int lane = threadIdx.x & 31;
+  const int P = A.pv.P;
+  const unsigned long long n_items = A.ctr->n_items;
+  while (true) {
+    unsigned long long item = 0;
+    int stop = 0;
+    if (lane == 0) {
+      stop = *A.abort_flag;
+      item = stop ? n_items : atomicAdd(&A.ctr->next_item, 1ull);
+    }
+    item = __shfl_sync(kFull, item, 0);
+    stop = __shfl_sync(kFull, stop, 0);
+    if (stop) {
+      if (lane == 0) A.ctr->status = DPG_ERR_ABORTED;
+      break;
+    }
+    if (item >= n_items) break;
+    // order position lo with ord_ibase[lo] <= item < ord_ibase[lo + 1]
+    int lo = 0, hi = P;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (A.ord_ibase[mid] <= item) lo = mid; else hi = mid;
+    }
+    const int p = A.pv.order[lo];
+    const unsigned long long j = item - A.ord_ibase[lo];
+    const unsigned long long first = A.ord_pbase[lo] + 32ull * j;
+    const unsigned long long end = A.ord_pbase[lo + 1];
+    const unsigned long long pair = first + lane;
+    const bool active = pair < end;
+    const uint32_t node = active ? A.out.node[pair] : 0u;
+    check_one<KIND, Real, BAND, CULL, true>(A, smem, p, (int64_t)pair, node, active);
+  }
+}
+
+}  // namespace dpg

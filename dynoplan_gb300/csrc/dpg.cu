@@ -12,7 +12,7 @@
 #include <vector>
 
 #include "dpg.h"
-#include "expand_kernels.cuh"
+#include "check_kernels.cuh"
 
 using namespace dpg;
 
@@ -38,8 +38,9 @@ struct dpg_ctx {
   int P = 0;
   int64_t S = 0, A = 0;
   std::vector<int32_t> h_len, h_order;
-  std::vector<int64_t> h_soff, h_aoff;
+  std::vector<int64_t> h_soff, h_aoff, h_coff;
   DevBuf len, soff, aoff, order, key32, kconst32, st64, st32, act64, pose32, pose64, pbox;
+  DevBuf coff, cbox32, tbox32;
 
   // environment
   bool have_env = false;
@@ -50,7 +51,7 @@ struct dpg_ctx {
 
   // per-call arena
   DevBuf x64, nkey32, noff32, mask, cnt, tot, pbase, ord_pbase, ord_ibase;
-  DevBuf p_node, p_prim, p_verdict, p_fi, p_end, p_gap, p_flags, p_recheck;
+  DevBuf p_node, p_prim, p_verdict, p_fi, p_end, p_gap, p_flags;
   DevCounters *d_ctr = nullptr;
   DevCounters *h_ctr = nullptr;  // pinned
   int *h_abort = nullptr;        // mapped pinned
@@ -244,7 +245,7 @@ void dpg_destroy(dpg_ctx *c) {
                     &c->st32, &c->act64, &c->pose32, &c->pose64, &c->pbox, &c->obs32, &c->obs64,
                     &c->x64, &c->nkey32, &c->noff32, &c->mask, &c->cnt, &c->tot, &c->pbase,
                     &c->ord_pbase, &c->ord_ibase, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
-                    &c->p_end, &c->p_gap, &c->p_flags, &c->p_recheck};
+                    &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32};
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
@@ -265,11 +266,14 @@ int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const doubl
   c->h_len.assign(len, len + P);
   c->h_soff.resize(P);
   c->h_aoff.resize(P);
-  int64_t S = 0, A = 0;
+  c->h_coff.resize(P);
+  int64_t S = 0, A = 0, NC = 0;
   for (int p = 0; p < P; p++) {
     if (len[p] < 1 || len[p] > 32767) return fail(c, DPG_ERR_ARG, "upload_primitives: length out of [1, 32767]");
     c->h_soff[p] = S;
     c->h_aoff[p] = A;
+    c->h_coff[p] = NC;
+    NC += (len[p] + kChunk - 1) / kChunk;
     S += len[p];
     A += len[p] - 1;
   }
@@ -291,13 +295,17 @@ int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const doubl
       (rc = ensure(c, c->act64, sizeof(double) * nu * std::max<int64_t>(A, 1))) ||
       (rc = ensure(c, c->pose32, sizeof(Pose<float>) * parts * S)) ||
       (rc = ensure(c, c->pose64, sizeof(Pose<double>) * parts * S)) ||
-      (rc = ensure(c, c->pbox, sizeof(double) * 2 * pd * P)))
+      (rc = ensure(c, c->pbox, sizeof(double) * 2 * pd * P)) ||
+      (rc = ensure(c, c->coff, sizeof(int64_t) * P)) ||
+      (rc = ensure(c, c->cbox32, sizeof(float) * 2 * pd * NC)) ||
+      (rc = ensure(c, c->tbox32, sizeof(float) * 2 * pd * P)))
     return rc;
   cudaStream_t st = c->stream;
   CUDA_TRY(c, cudaMemcpyAsync(c->len.p, len, sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->soff.p, c->h_soff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->aoff.p, c->h_aoff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->order.p, c->h_order.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->coff.p, c->h_coff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->st64.p, states, sizeof(double) * nx * S, cudaMemcpyHostToDevice, st));
   if (A > 0)
     CUDA_TRY(c, cudaMemcpyAsync(c->act64.p, actions, sizeof(double) * nu * A, cudaMemcpyHostToDevice, st));
@@ -314,6 +322,9 @@ int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const doubl
     build_keys<KIND><<<(P + 127) / 128, 128, 0, st>>>(rp, P, P_<int32_t>(c->len), P_<int64_t>(c->soff),
                                                        P_<double>(c->st64), P_<float>(c->key32),
                                                        P_<float>(c->kconst32), P_<double>(c->pbox));
+    build_chunks<KIND><<<(P + 127) / 128, 128, 0, st>>>(rp, P, P_<int32_t>(c->len), P_<int64_t>(c->soff),
+                                                         P_<int64_t>(c->coff), P_<Pose<double>>(c->pose64), S,
+                                                         P_<float>(c->cbox32), P_<float>(c->tbox32));
   });
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaStreamSynchronize(st));
@@ -451,8 +462,6 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     pv_out.min_gap = out->min_gap ? P_<float>(c->p_gap) : nullptr;
     pv_out.flags = out->flags ? P_<uint8_t>(c->p_flags) : nullptr;
   }
-  if ((rc = ensure(c, c->p_recheck, 4 * capz))) return rc;
-  pv_out.recheck = P_<uint32_t>(c->p_recheck);
 
   CUDA_TRY(c, cudaEventRecord(c->ev[0], st));
   if (N > 0) {
@@ -477,6 +486,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   pv.pose32 = P_<Pose<float>>(c->pose32);
   pv.pose64 = P_<Pose<double>>(c->pose64);
   pv.pbox = P_<double>(c->pbox);
+  pv.coff = P_<int64_t>(c->coff);
+  pv.cbox32 = P_<float>(c->cbox32);
+  pv.tbox32 = P_<float>(c->tbox32);
   NodeView nv{N, P_<double>(c->x64), P_<float>(c->nkey32), P_<float>(c->noff32)};
   EnvView ev{};
   ev.dim = c->dim;
@@ -500,6 +512,10 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   ca.ctr = ctr;
   ca.abort_flag = c->d_abort;
   ca.band = fp64 ? 0.0 : band;
+  // culling keeps every obstacle within the min_gap cap, the FP64 band and a
+  // slack for the FP32 box arithmetic
+  ca.cull_margin = kGapCap + (float)band + 1e-3f;
+  const bool cull = c->n_obs <= kMaxCullObs;
 
   cudaError_t launch_err = cudaSuccess;
   with_kind(kind, [&](auto K) {
@@ -526,28 +542,21 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     // exact check: persistent grid, obstacles in shared memory
     const size_t obs_bytes32 = R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>);
     const size_t obs_bytes64 = R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>);
+    auto launch = [&](auto kern, size_t obs_bytes) {
+      const size_t sm = obs_bytes * std::max(c->n_obs, 1);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
+      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+    };
     if (fp64) {
-      auto kern = check_pairs<KIND, double, false>;
-      const size_t sm = obs_bytes64 * std::max(c->n_obs, 1);
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      int per_sm = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
-      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+      if (cull) launch(check_pairs<KIND, double, false, true>, obs_bytes64);
+      else launch(check_pairs<KIND, double, false, false>, obs_bytes64);
     } else {
-      auto kern = check_pairs<KIND, float, true>;
-      const size_t sm = obs_bytes32 * std::max(c->n_obs, 1);
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      int per_sm = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
-      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+      if (cull) launch(check_pairs<KIND, float, true, true>, obs_bytes32);
+      else launch(check_pairs<KIND, float, true, false>, obs_bytes32);
     }
     cudaEventRecord(c->ev[3], st);
-    if (!fp64) {
-      auto rk = recheck_pairs<KIND>;
-      const size_t sm = obs_bytes64 * std::max(c->n_obs, 1);
-      cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      rk<<<c->sm_count * 2, kCheckThreads, sm, st>>>(ca);
-    }
     cudaEventRecord(c->ev[4], st);
     launch_err = cudaGetLastError();
   });

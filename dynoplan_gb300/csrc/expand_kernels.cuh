@@ -8,7 +8,7 @@
 //   scan_totals     per-primitive bases in length order, work-item bases
 //   nn_emit         pair lists grouped by primitive, nodes ascending
 //   check_pairs     persistent warps over (primitive, 32 nodes) work items
-//   recheck_pairs   FP64 re-check of pairs flagged near contact or bounds
+//                   (check_kernels.cuh)
 //
 // The reference does this per node with a KD-tree radius query and a
 // per-motion fcl AABB tree (include/dynoplan/dbastar/dbastar.hpp:270-312,
@@ -30,6 +30,9 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kNNThreads = 256;   // 8 warps = 8 bitmask words = 256 nodes
 constexpr int kNNTile = 256;      // primitives staged per shared-memory tile
 constexpr int kCheckThreads = 256;
+constexpr int kChunk = 8;          // states per culling chunk
+constexpr int kMaxCullObs = 128;   // per-lane candidate bitmask covers this many obstacles
+constexpr float kGapCap = 0.05f;   // min_gap is exact up to this clearance, +inf above
 
 struct DevCounters {
   unsigned long long n_pairs;
@@ -59,7 +62,11 @@ struct PrimView {
   const float *st32;         // [S][NX]
   const Pose<float> *pose32; // [PARTS][S] (3-D: cx,cy,c = position, s unused)
   const Pose<double> *pose64;
-  const double *pbox;        // [P][2*POSD]: lo..., hi...
+  const double *pbox;        // [P][2*POSD]: lo..., hi... of the state positions
+  const int64_t *coff;       // [P] first chunk row of primitive p
+  const float *cbox32;       // [sum chunks][2*POSD]: centre..., half... of the parts'
+                             //   bounding box over kChunk states (outward rounded)
+  const float *tbox32;       // [P][2*POSD]: the same over the whole primitive
 };
 
 struct NodeView {
@@ -86,7 +93,6 @@ struct PairView {
   void *end_state;     // float or double rows of NX
   float *min_gap;
   uint8_t *flags;
-  uint32_t *recheck;   // pair indices flagged for the FP64 re-check
 };
 
 __device__ __forceinline__ float wrap_pi_f64(double a) {
@@ -296,311 +302,6 @@ __global__ void __launch_bounds__(256) nn_emit(int P, int Ppad, int64_t W, const
   }
 }
 
-// ------------------------------------------------------ exact checking ---
-
-template <class Real> struct StepGeom {
-  // per state, per part: pose and its axis-aligned half extents
-  Real cx[2], cy[2], c[2], s[2], ex[2], ey[2];
-};
-
-// Collision test of one state against all obstacles (planar box parts).
-// Updates the lane's min axis-aligned clearance; returns 0 clear, 1 hit,
-// 2 ambiguous (|gap| <= band, FP32 path only).
-template <class Real, bool BAND, int PARTS>
-__device__ __forceinline__ int test_planar(const StepGeom<Real> &G, Real px0, Real py0, Real px1,
-                                           Real py1, const Obs2<Real> *obs, int n_obs, Real a,
-                                           Real b, Real band, Real &mg) {
-  int res = 0;
-  for (int o = 0; o < n_obs; o++) {
-    const Obs2<Real> ob = obs[o];
-#pragma unroll
-    for (int q = 0; q < PARTS; q++) {
-      const Real px = q == 0 ? px0 : px1, py = q == 0 ? py0 : py1;
-      const Real dx = px - ob.cx, dy = py - ob.cy;
-      const Real g = fmax(fabs(dx) - (G.ex[q] + ob.hx), fabs(dy) - (G.ey[q] + ob.hy));
-      mg = fmin(mg, g);
-      if (g <= band) {
-        const Real ac = fabs(G.c[q]), as = fabs(G.s[q]);
-        const Real du = dx * G.c[q] + dy * G.s[q], dv = dy * G.c[q] - dx * G.s[q];
-        const Real gu = fabs(du) - (a + ob.hx * ac + ob.hy * as);
-        const Real gv = fabs(dv) - (b + ob.hx * as + ob.hy * ac);
-        const Real gs = fmax(g, fmax(gu, gv));
-        if (BAND) {
-          if (gs <= band) res = max(res, gs < -band ? 1 : 2);
-        } else {
-          if (gs <= Real(0)) res = 1;
-        }
-      }
-    }
-  }
-  return res;
-}
-
-template <class Real, bool BAND>
-__device__ __forceinline__ int test_sphere(Real px, Real py, Real pz, const Obs3<Real> *obs,
-                                           int n_obs, Real rad, Real band, Real &mg) {
-  int res = 0;
-  for (int o = 0; o < n_obs; o++) {
-    const Obs3<Real> ob = obs[o];
-    const Real dx = fabs(px - ob.cx) - ob.hx, dy = fabs(py - ob.cy) - ob.hy,
-               dz = fabs(pz - ob.cz) - ob.hz;
-    const Real m = fmax(dx, fmax(dy, dz));
-    const Real g = m - rad;
-    mg = fmin(mg, g);
-    if (g <= band) {
-      const Real ux = fmax(dx, Real(0)), uy = fmax(dy, Real(0)), uz = fmax(dz, Real(0));
-      const Real gs = (m <= Real(0) ? m : sqrt(ux * ux + uy * uy + uz * uz)) - rad;
-      if (BAND) {
-        if (gs <= band) res = max(res, gs < -band ? 1 : 2);
-      } else {
-        if (gs <= Real(0)) res = 1;
-      }
-    }
-  }
-  return res;
-}
-
-// bounds of a position component: 0 inside, 1 outside, 2 ambiguous
-template <class Real, bool BAND>
-__device__ __forceinline__ int bound_test(Real v, double lo, double hi, Real band) {
-  if (BAND) {
-    if (v < Real(lo) - band || v > Real(hi) + band) return 1;
-    if (v <= Real(lo) + band || v >= Real(hi) - band) return 2;
-    return 0;
-  } else {
-    return (v >= Real(lo) && v <= Real(hi)) ? 0 : 1;
-  }
-}
-
-struct CheckArgs {
-  RobotParams rp;
-  PrimView pv;
-  NodeView nv;
-  EnvView ev;
-  PairView out;
-  const unsigned long long *ord_pbase;
-  const unsigned long long *ord_ibase;
-  DevCounters *ctr;
-  const volatile int *abort_flag;
-  double band;
-};
-
-template <class Real> __device__ __forceinline__ const Pose<Real> *pose_table(const PrimView &pv);
-template <> __device__ __forceinline__ const Pose<float> *pose_table<float>(const PrimView &pv) { return pv.pose32; }
-template <> __device__ __forceinline__ const Pose<double> *pose_table<double>(const PrimView &pv) { return pv.pose64; }
-
-template <class Real> __device__ __forceinline__ Real node_off(const NodeView &nv, int64_t n, int i, int nx, int comp);
-template <> __device__ __forceinline__ float node_off<float>(const NodeView &nv, int64_t n, int i, int nx, int comp) {
-  return nv.off32[i * nv.N + n];
-}
-template <> __device__ __forceinline__ double node_off<double>(const NodeView &nv, int64_t n, int i, int nx, int comp) {
-  return nv.x64[n * nx + comp];
-}
-
-// One (primitive, node) pair: the transformed trajectory is
-//   position_k = canonical_k + offset_pos + k*dt*offset_vel,
-//   velocity_k = canonical_k + offset_vel, other components = canonical_k,
-// which is the translation of the stored states (unicycle1, car1) and the
-// exact re-rollout from the shifted start (quad2d, quad3d: no dynamics term
-// depends on position or velocity).  LOCKSTEP: the 32 lanes of a warp share
-// the primitive and advance over its states together.
-template <int KIND, class Real, bool BAND, bool LOCKSTEP, class OutT>
-__device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t pair,
-                          uint32_t node, bool active, uint8_t flag_bits) {
-  using R = Robot<KIND>;
-  const PrimView &pv = A.pv;
-  const RobotParams &rp = A.rp;
-  const int L = pv.len[p];
-  const int64_t s0 = pv.soff[p];
-  const Pose<Real> *pose = pose_table<Real>(pv);
-  const Real band = BAND ? Real(A.band) : Real(0);
-
-  Real off[R::POSD + R::VELOFF];
-#pragma unroll
-  for (int i = 0; i < R::POSD; i++) off[i] = active ? node_off<Real>(A.nv, node, i, R::NX, i) : Real(0);
-#pragma unroll
-  for (int i = 0; i < R::VELOFF; i++)
-    off[R::POSD + i] = active ? node_off<Real>(A.nv, node, R::POSD + i, R::NX, R::vel_comp(i)) : Real(0);
-
-  // bounds pre-check on the swept box of the trajectory (FP64)
-  bool need_bounds = true;
-  if (active) {
-    const double *bx = pv.pbox + (int64_t)p * 2 * R::POSD;
-    const double *x64 = A.nv.x64 + (int64_t)node * R::NX;
-    const double tmax = (L - 1) * rp.dt;
-    bool inside = true;
-#pragma unroll
-    for (int i = 0; i < R::POSD; i++) {
-      double lo = bx[i] + x64[i], hi = bx[R::POSD + i] + x64[i];
-      if (R::VELOFF) {
-        const double sv = tmax * x64[R::vel_comp(i)];
-        lo += fmin(sv, 0.0);
-        hi += fmax(sv, 0.0);
-      }
-      inside = inside && lo > A.ev.lo[i] + A.band && hi < A.ev.hi[i] - A.band;
-    }
-    need_bounds = !inside;
-  }
-
-  bool done = !active, collided = false;
-  int first_oob = L, first_col = L, amb = 0;
-  Real mg = Real(INFINITY);  // no obstacle: +inf
-  const Real hl = Real(rp.half_len), hw = Real(rp.half_wid), rad = Real(rp.radius);
-
-  for (int k = 0; k < L; k++) {
-    if (LOCKSTEP) {
-      if (!__any_sync(kFull, !done)) break;
-    } else if (done) {
-      break;
-    }
-    // per-state geometry, shared by all lanes of the warp
-    StepGeom<Real> G;
-#pragma unroll
-    for (int q = 0; q < R::PARTS; q++) {
-      const Pose<Real> ps = pose[q * pv.S + s0 + k];
-      G.cx[q] = ps.cx; G.cy[q] = ps.cy; G.c[q] = ps.c; G.s[q] = ps.s;
-      if (!R::SPHERE) {
-        const Real ac = fabs(ps.c), as = fabs(ps.s);
-        G.ex[q] = hl * ac + hw * as;
-        G.ey[q] = hl * as + hw * ac;
-      }
-    }
-    if (done) continue;
-    const Real t = Real(k) * Real(rp.dt);
-    Real sx = off[0], sy = off[1], sz = Real(0);
-    if (R::VELOFF) { sx += t * off[R::POSD + 0]; sy += t * off[R::POSD + 1]; }
-    if (R::POSD == 3) { sz = off[2]; if (R::VELOFF) sz += t * off[R::POSD + 2]; }
-    const Real px0 = G.cx[0] + sx, py0 = G.cy[0] + sy;
-    if (need_bounds) {
-      int bt = bound_test<Real, BAND>(px0, A.ev.lo[0], A.ev.hi[0], band);
-      bt = max(bt, bound_test<Real, BAND>(py0, A.ev.lo[1], A.ev.hi[1], band));
-      if (R::POSD == 3) bt = max(bt, bound_test<Real, BAND>(G.c[0] + sz, A.ev.lo[2], A.ev.hi[2], band));
-      if (bt == 2) { amb = 1; done = true; continue; }
-      if (bt == 1) { first_oob = k; done = true; continue; }
-    }
-    if (collided) continue;
-    int res;
-    if constexpr (R::SPHERE) {
-      res = test_sphere<Real, BAND>(px0, py0, G.c[0] + sz, (const Obs3<Real> *)obs_sm, A.ev.n_obs, rad, band, mg);
-    } else {
-      const Real px1 = R::PARTS > 1 ? G.cx[R::PARTS - 1] + sx : px0;
-      const Real py1 = R::PARTS > 1 ? G.cy[R::PARTS - 1] + sy : py0;
-      res = test_planar<Real, BAND, R::PARTS>(G, px0, py0, px1, py1, (const Obs2<Real> *)obs_sm,
-                                              A.ev.n_obs, hl, hw, band, mg);
-    }
-    if (res == 2) { amb = 1; done = true; continue; }
-    if (res == 1) {
-      collided = true;
-      first_col = k;
-      if (!need_bounds) done = true;
-    }
-  }
-  if (!active) return;
-  const PairView &o = A.out;
-  if (amb) {  // hand the pair to the FP64 re-check
-    const unsigned long long slot = atomicAdd(&A.ctr->n_recheck, 1ull);
-    o.recheck[slot] = (uint32_t)pair;
-    return;
-  }
-  uint8_t verdict;
-  int fi;
-  if (first_oob < L) { verdict = DPG_OUT_OF_BOUNDS; fi = first_oob; }
-  else if (collided) { verdict = DPG_COLLISION; fi = first_col; }
-  else { verdict = DPG_VALID; fi = L; }
-  const int er = first_oob < L ? first_oob : L - 1;  // end-state row
-  if (o.verdict) o.verdict[pair] = verdict;
-  if (o.first_invalid) o.first_invalid[pair] = (int16_t)fi;
-  if (o.min_gap) o.min_gap[pair] = verdict == DPG_OUT_OF_BOUNDS ? __int_as_float(0x7fc00000) : (float)mg;
-  if (o.flags) o.flags[pair] = flag_bits;
-  if (o.end_state) {
-    OutT *es = (OutT *)o.end_state + pair * R::NX;
-    const Real t = Real(er) * Real(rp.dt);
-    const int64_t row = s0 + er;
-#pragma unroll
-    for (int c = 0; c < R::NX; c++) {
-      Real v = sizeof(Real) == 4 ? Real(pv.st32[row * R::NX + c]) : Real(pv.st64[row * R::NX + c]);
-      if (c < R::POSD) {
-        v += off[c];
-        if (R::VELOFF) v += t * off[R::POSD + c];
-      }
-#pragma unroll
-      for (int i = 0; i < R::VELOFF; i++)
-        if (c == R::vel_comp(i)) v += off[R::POSD + i];
-      es[c] = (OutT)v;
-    }
-  }
-}
-
-template <class Real, int KIND>
-__device__ void load_obstacles(const EnvView &ev, void *sm) {
-  using R = Robot<KIND>;
-  if constexpr (R::SPHERE) {
-    const Obs3<Real> *src = (const Obs3<Real> *)(sizeof(Real) == 4 ? ev.obs32 : ev.obs64);
-    Obs3<Real> *dst = (Obs3<Real> *)sm;
-    for (int i = threadIdx.x; i < ev.n_obs; i += blockDim.x) dst[i] = src[i];
-  } else {
-    const Obs2<Real> *src = (const Obs2<Real> *)(sizeof(Real) == 4 ? ev.obs32 : ev.obs64);
-    Obs2<Real> *dst = (Obs2<Real> *)sm;
-    for (int i = threadIdx.x; i < ev.n_obs; i += blockDim.x) dst[i] = src[i];
-  }
-  __syncthreads();
-}
-
-// Persistent warps: each warp takes the next work item (primitive in order
-// of decreasing length, next 32 of its nodes) from a device counter.
-template <int KIND, class Real, bool BAND>
-__global__ void __launch_bounds__(kCheckThreads) check_pairs(CheckArgs A) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  load_obstacles<Real, KIND>(A.ev, smem);
-  const int lane = threadIdx.x & 31;
-  const int P = A.pv.P;
-  const unsigned long long n_items = A.ctr->n_items;
-  while (true) {
-    unsigned long long item = 0;
-    int stop = 0;
-    if (lane == 0) {
-      stop = *A.abort_flag;
-      item = stop ? n_items : atomicAdd(&A.ctr->next_item, 1ull);
-    }
-    item = __shfl_sync(kFull, item, 0);
-    stop = __shfl_sync(kFull, stop, 0);
-    if (stop) {
-      if (lane == 0) A.ctr->status = DPG_ERR_ABORTED;
-      break;
-    }
-    if (item >= n_items) break;
-    // order position i with ord_ibase[i] <= item < ord_ibase[i+1]
-    int lo = 0, hi = P;  // invariant: ord_ibase[lo] <= item < ord_ibase[hi]
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (A.ord_ibase[mid] <= item) lo = mid; else hi = mid;
-    }
-    const int p = A.pv.order[lo];
-    const unsigned long long j = item - A.ord_ibase[lo];
-    const unsigned long long first = A.ord_pbase[lo] + 32ull * j;
-    const unsigned long long end = A.ord_pbase[lo + 1];
-    const unsigned long long pair = first + lane;
-    const bool active = pair < end;
-    const uint32_t node = active ? A.out.node[pair] : 0u;
-    check_one<KIND, Real, BAND, true, Real>(A, smem, p, (int64_t)pair, node, active, 0);
-  }
-}
-
-// FP64 re-check of flagged pairs, one thread per pair.
-template <int KIND>
-__global__ void __launch_bounds__(kCheckThreads) recheck_pairs(CheckArgs A) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  load_obstacles<double, KIND>(A.ev, smem);
-  const unsigned long long n = A.ctr->n_recheck;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    const uint32_t pair = A.out.recheck[i];
-    const int p = (int)A.out.prim[pair];
-    check_one<KIND, double, false, false, float>(A, smem, p, pair, A.out.node[pair], true,
-                                          DPG_FLAG_CONTACT_RECHECK);
-  }
-}
-
 // --------------------------------------------------- upload-time tables ---
 
 // Canonical FP64 rollout of every primitive from its stored start with its
@@ -677,6 +378,58 @@ __global__ void build_keys(RobotParams rp, int P, const int32_t *len, const int6
   for (int i = 0; i < R::POSD; i++) {
     pbox[(int64_t)p * 2 * R::POSD + i] = lo[i];
     pbox[(int64_t)p * 2 * R::POSD + R::POSD + i] = hi[i];
+  }
+}
+
+// Culling boxes: per chunk of kChunk states, the bounding box of every
+// collision part over those canonical states; per primitive, the union.
+// FP64, then rounded outward to FP32 (centre to nearest, half extent up by
+// the centre's rounding error).
+template <int KIND>
+__global__ void build_chunks(RobotParams rp, int P, const int32_t *len, const int64_t *soff,
+                             const int64_t *coff, const Pose<double> *pose64, int64_t S,
+                             float *cbox32, float *tbox32) {
+  using R = Robot<KIND>;
+  constexpr int D = R::POSD;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double tlo[3] = {1e300, 1e300, 1e300}, thi[3] = {-1e300, -1e300, -1e300};
+  const int L = len[p];
+  for (int c = 0; c * kChunk < L; c++) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int k = c * kChunk; k < min(L, (c + 1) * kChunk); k++) {
+      for (int q = 0; q < R::PARTS; q++) {
+        const Pose<double> ps = pose64[q * S + soff[p] + k];
+        if constexpr (R::SPHERE) {
+          const double v[3] = {ps.cx, ps.cy, ps.c};
+          for (int i = 0; i < 3; i++) {
+            lo[i] = fmin(lo[i], v[i] - rp.radius);
+            hi[i] = fmax(hi[i], v[i] + rp.radius);
+          }
+        } else {
+          const double ac = fabs(ps.c), as = fabs(ps.s);
+          const double ex = rp.half_len * ac + rp.half_wid * as, ey = rp.half_len * as + rp.half_wid * ac;
+          lo[0] = fmin(lo[0], ps.cx - ex); hi[0] = fmax(hi[0], ps.cx + ex);
+          lo[1] = fmin(lo[1], ps.cy - ey); hi[1] = fmax(hi[1], ps.cy + ey);
+        }
+      }
+    }
+    float *cb = cbox32 + (coff[p] + c) * 2 * D;
+    for (int i = 0; i < D; i++) {
+      const double cen = 0.5 * (lo[i] + hi[i]), half = 0.5 * (hi[i] - lo[i]);
+      const float c32 = (float)cen;
+      cb[i] = c32;
+      cb[D + i] = __double2float_ru(half + fabs(cen - (double)c32));
+      tlo[i] = fmin(tlo[i], lo[i]);
+      thi[i] = fmax(thi[i], hi[i]);
+    }
+  }
+  float *tb = tbox32 + (int64_t)p * 2 * D;
+  for (int i = 0; i < D; i++) {
+    const double cen = 0.5 * (tlo[i] + thi[i]), half = 0.5 * (thi[i] - tlo[i]);
+    const float c32 = (float)cen;
+    tb[i] = c32;
+    tb[D + i] = __double2float_ru(half + fabs(cen - (double)c32));
   }
 }
 

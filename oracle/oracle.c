@@ -442,12 +442,12 @@ int orc_check_pair(const orc_robot *r, const orc_env *e, const orc_prims *pr,
     }
     if (hit) {
       *first_invalid = (int16_t)s;
-      *min_gap = mg;
+      *min_gap = mg <= ORC_GAP_CAP ? mg : INFINITY;
       return ORC_COLLISION;
     }
   }
   *first_invalid = (int16_t)L;
-  *min_gap = mg;
+  *min_gap = mg <= ORC_GAP_CAP ? mg : INFINITY;
   return ORC_VALID;
 }
 

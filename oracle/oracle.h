@@ -43,6 +43,10 @@ extern "C" {
 #endif
 
 enum { ORC_UNICYCLE1 = 0, ORC_CAR1 = 1, ORC_QUAD3D = 2, ORC_QUAD2D = 3 };
+
+/* min_gap is the min axis-aligned clearance along the checked states when
+ * that is <= ORC_GAP_CAP metres, +inf otherwise (NaN for out-of-bounds). */
+#define ORC_GAP_CAP 0.05
 enum { ORC_VALID = 0, ORC_COLLISION = 1, ORC_OUT_OF_BOUNDS = 2 };
 
 /* Robot description; the field meaning is identical to dpg_robot_desc in

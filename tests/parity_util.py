@@ -14,6 +14,7 @@ import numpy as np
 from dynoplan_gb300 import workloads as W
 
 ANGLE_COMPS = {W.UNICYCLE1: [2], W.CAR1: [2, 3], W.QUAD2D: [2], W.QUAD3D: []}
+GAP_CAP = 0.05  # min_gap is reported up to this clearance, +inf above
 
 
 def sort_by_pair(res):
@@ -45,9 +46,16 @@ def compare(kind, gpu, ora, precision, min_gap=True):
     assert not bad.any(), f"end state mismatch at {np.argwhere(bad)[:5].tolist()}: max {np.abs(d).max()}"
     out = {"end_state_max_abs": float(np.abs(d).max()) if len(d) else 0.0}
     if min_gap and len(d):
-        fin = np.isfinite(o["min_gap"])
-        np.testing.assert_array_equal(np.isfinite(g["min_gap"]), fin)
-        gm = np.abs(g["min_gap"][fin].astype(np.float64) - o["min_gap"][fin])
-        assert gm.max(initial=0) <= (1e-5 if precision == 1 else 2e-4), gm.max(initial=0)
-        out["min_gap_max_abs"] = float(gm.max(initial=0))
+        tol = 1e-5 if precision == 1 else 2e-4
+        gg, og = g["min_gap"].astype(np.float64), o["min_gap"]
+        # NaN (out of bounds) on the same rows
+        np.testing.assert_array_equal(np.isnan(gg), np.isnan(og))
+        # +inf = clearance above the 5 cm cap; a value within tol of the cap
+        # may fall on either side
+        near_cap = lambda v: np.isinf(v) | (v >= GAP_CAP - tol)
+        both = np.isfinite(gg) & np.isfinite(og)
+        ok =np.where(np.isnan(og), True,
+                      np.where(both, np.abs(gg - og) <= tol, near_cap(gg) & near_cap(og)))
+        assert ok.all(), f"min_gap mismatch at {np.argwhere(~ok)[:5].ravel().tolist()}"
+        out["min_gap_max_abs"] = float(np.abs(gg[both] - og[both]).max(initial=0))
     return out
