@@ -43,6 +43,10 @@ struct CheckArgs {
   const volatile int *abort_flag;
   double band;       // FP64 re-check band (0 on the FP64 path)
   float cull_margin; // obstacle culling margin
+  // FP32 copies of the constants the state loop uses (GB300 runs FP64 and
+  // double->float conversions at 1/64 of the FP32 rate)
+  float dt32, half_len32, half_wid32, radius32, band32;
+  float lo32[3], hi32[3];
 };
 
 template <class Real> __device__ __forceinline__ const Pose<Real> *pose_table(const PrimView &pv);
@@ -172,7 +176,15 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   const int L = pv.len[p];
   const int64_t s0 = pv.soff[p];
   const Pose<Real> *pose = pose_table<Real>(pv);
-  const Real band = BAND ? Real(A.band) : Real(0);
+  constexpr bool F32 = sizeof(Real) == 4;
+  const Real band = BAND ? (F32 ? Real(A.band32) : Real(A.band)) : Real(0);
+  const Real dtR = F32 ? Real(A.dt32) : Real(rp.dt);
+  Real loR[3], hiR[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    loR[i] = F32 ? Real(A.lo32[i]) : Real(A.ev.lo[i]);
+    hiR[i] = F32 ? Real(A.hi32[i]) : Real(A.ev.hi[i]);
+  }
   const double *x64 = A.nv.x64 + (int64_t)(active ? node : 0) * R::NX;
   const int n_obs = A.ev.n_obs;
 
@@ -182,21 +194,25 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
 #pragma unroll
   for (int i = 0; i < V; i++) off[D + i] = active ? node_off<Real>(A.nv, node, D + i, R::NX, R::vel_comp(i)) : Real(0);
 
-  // bounds pre-check on the swept box of the positions (FP64)
+  // bounds pre-check on the swept box of the positions: inside with a margin
+  // (band + slack for the arithmetic) means no state needs a bounds test
   bool need_bounds = true;
   if (active) {
     const double *bx = pv.pbox + (int64_t)p * 2 * D;
-    const double tmax = (L - 1) * rp.dt;
+    const float *bx32 = pv.pbox32 + (int64_t)p * 2 * D;
+    const Real tmax = Real(L - 1) * dtR;
+    const Real slack = F32 ? Real(1e-3f) : Real(0);
     bool inside = true;
 #pragma unroll
     for (int i = 0; i < D; i++) {
-      double lo = bx[i] + x64[i], hi = bx[D + i] + x64[i];
+      Real lo = (F32 ? Real(bx32[i]) : Real(bx[i])) + off[i];
+      Real hi = (F32 ? Real(bx32[D + i]) : Real(bx[D + i])) + off[i];
       if (V) {
-        const double sv = tmax * x64[R::vel_comp(i)];
-        lo += fmin(sv, 0.0);
-        hi += fmax(sv, 0.0);
+        const Real sv = tmax * off[D + i];
+        lo += fmin(sv, Real(0));
+        hi += fmax(sv, Real(0));
       }
-      inside = inside && lo > A.ev.lo[i] + A.band && hi < A.ev.hi[i] - A.band;
+      inside = inside && lo > loR[i] + band + slack && hi < hiR[i] - band - slack;
     }
     need_bounds = !inside;
   }
@@ -206,7 +222,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   const float M = A.cull_margin;
   if (CULL && active) {
     const float *tb = pv.tbox32 + (int64_t)p * 2 * D;
-    const float tmax = float(L - 1) * float(rp.dt);
+    const float tmax = float(L - 1) * A.dt32;
     float cen[D], hf[D];
 #pragma unroll
     for (int i = 0; i < D; i++) {
@@ -225,7 +241,9 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   bool done = !active, collided = false, rechecked = false;
   int first_oob = L, first_col = L;
   Real mg = Real(INFINITY);
-  const Real hl = Real(rp.half_len), hw = Real(rp.half_wid), rad = Real(rp.radius);
+  const Real hl = F32 ? Real(A.half_len32) : Real(rp.half_len);
+  const Real hw = F32 ? Real(A.half_wid32) : Real(rp.half_wid);
+  const Real rad = F32 ? Real(A.radius32) : Real(rp.radius);
   uint32_t cm[kMaxCullObs / 32] = {0u, 0u, 0u, 0u};
 
   for (int k = 0; k < L; k++) {
@@ -234,11 +252,11 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
     } else if (done) {
       break;
     }
-    const Real t = Real(k) * Real(rp.dt);
+    const Real t = Real(k) * dtR;
     // level-2 culling at each chunk start
     if (CULL && (k % kChunk) == 0 && !done && !collided) {
       const float *cb = pv.cbox32 + (pv.coff[p] + k / kChunk) * 2 * D;
-      const float t0 = float(k) * float(rp.dt), t1 = float(min(L - 1, k + kChunk - 1)) * float(rp.dt);
+      const float t0 = float(k) * A.dt32, t1 = float(min(L - 1, k + kChunk - 1)) * A.dt32;
       float cen[D], hf[D];
 #pragma unroll
       for (int i = 0; i < D; i++) {
@@ -277,7 +295,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
         int r;
         if (BAND) {
           const Real v = pv3[i];
-          const Real lo = Real(A.ev.lo[i]), hi = Real(A.ev.hi[i]);
+          const Real lo = loR[i], hi = hiR[i];
           r = (v < lo - band || v > hi + band) ? 1 : ((v <= lo + band || v >= hi - band) ? 2 : 0);
           if (r == 2) {  // decide in FP64
             const double v64 = pos64<KIND>(A, s0 + k, k, x64, i);
@@ -285,7 +303,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
             rechecked = true;
           }
         } else {
-          r = (pv3[i] >= Real(A.ev.lo[i]) && pv3[i] <= Real(A.ev.hi[i])) ? 0 : 1;
+          r = (pv3[i] >= loR[i] && pv3[i] <= hiR[i]) ? 0 : 1;
         }
         bt |= r;
       }
@@ -350,7 +368,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   if (o.flags) o.flags[pair] = rechecked ? DPG_FLAG_CONTACT_RECHECK : 0;
   if (o.end_state) {
     Real *es = (Real *)o.end_state + pair * R::NX;
-    const Real t = Real(er) * Real(rp.dt);
+    const Real t = Real(er) * dtR;
     const int64_t row = s0 + er;
 #pragma unroll
     for (int c = 0; c < R::NX; c++) {
@@ -384,7 +402,7 @@ __device__ void load_obstacles(const EnvView &ev, void *sm) {
 
 // Persistent warps over (primitive, 32 nodes) work items.
 template <int KIND, class Real, bool BAND, bool CULL>
-__global__ void __launch_bounds__(kCheckThreads) check_pairs(CheckArgs A) {
+__global__ void __launch_bounds__(kCheckThreads, 4) check_pairs(CheckArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   load_obstacles<Real, KIND>(A.ev, smem);
   const int lane = threadIdx.x & 31;

@@ -39,7 +39,7 @@ struct dpg_ctx {
   int64_t S = 0, A = 0;
   std::vector<int32_t> h_len, h_order;
   std::vector<int64_t> h_soff, h_aoff, h_coff;
-  DevBuf len, soff, aoff, order, key32, kconst32, st64, st32, act64, pose32, pose64, pbox;
+  DevBuf len, soff, aoff, order, key32, kconst32, st64, st32, act64, pose32, pose64, pbox, pbox32;
   DevBuf coff, cbox32, tbox32;
 
   // environment
@@ -242,7 +242,7 @@ void dpg_destroy(dpg_ctx *c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   DevBuf *bufs[] = {&c->len, &c->soff, &c->aoff, &c->order, &c->key32, &c->kconst32, &c->st64,
-                    &c->st32, &c->act64, &c->pose32, &c->pose64, &c->pbox, &c->obs32, &c->obs64,
+                    &c->st32, &c->act64, &c->pose32, &c->pose64, &c->pbox, &c->pbox32, &c->obs32, &c->obs64,
                     &c->x64, &c->nkey32, &c->noff32, &c->mask, &c->cnt, &c->tot, &c->pbase,
                     &c->ord_pbase, &c->ord_ibase, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
                     &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32};
@@ -296,6 +296,7 @@ int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const doubl
       (rc = ensure(c, c->pose32, sizeof(Pose<float>) * parts * S)) ||
       (rc = ensure(c, c->pose64, sizeof(Pose<double>) * parts * S)) ||
       (rc = ensure(c, c->pbox, sizeof(double) * 2 * pd * P)) ||
+      (rc = ensure(c, c->pbox32, sizeof(float) * 2 * pd * P)) ||
       (rc = ensure(c, c->coff, sizeof(int64_t) * P)) ||
       (rc = ensure(c, c->cbox32, sizeof(float) * 2 * pd * NC)) ||
       (rc = ensure(c, c->tbox32, sizeof(float) * 2 * pd * P)))
@@ -321,7 +322,8 @@ int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const doubl
                                                                   P_<Pose<float>>(c->pose32), P_<float>(c->st32));
     build_keys<KIND><<<(P + 127) / 128, 128, 0, st>>>(rp, P, P_<int32_t>(c->len), P_<int64_t>(c->soff),
                                                        P_<double>(c->st64), P_<float>(c->key32),
-                                                       P_<float>(c->kconst32), P_<double>(c->pbox));
+                                                       P_<float>(c->kconst32), P_<double>(c->pbox),
+                                                       P_<float>(c->pbox32));
     build_chunks<KIND><<<(P + 127) / 128, 128, 0, st>>>(rp, P, P_<int32_t>(c->len), P_<int64_t>(c->soff),
                                                          P_<int64_t>(c->coff), P_<Pose<double>>(c->pose64), S,
                                                          P_<float>(c->cbox32), P_<float>(c->tbox32));
@@ -486,6 +488,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   pv.pose32 = P_<Pose<float>>(c->pose32);
   pv.pose64 = P_<Pose<double>>(c->pose64);
   pv.pbox = P_<double>(c->pbox);
+  pv.pbox32 = P_<float>(c->pbox32);
   pv.coff = P_<int64_t>(c->coff);
   pv.cbox32 = P_<float>(c->cbox32);
   pv.tbox32 = P_<float>(c->tbox32);
@@ -515,6 +518,12 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   // culling keeps every obstacle within the min_gap cap, the FP64 band and a
   // slack for the FP32 box arithmetic
   ca.cull_margin = kGapCap + (float)band + 1e-3f;
+  ca.dt32 = (float)rp.dt;
+  ca.half_len32 = (float)rp.half_len;
+  ca.half_wid32 = (float)rp.half_wid;
+  ca.radius32 = (float)rp.radius;
+  ca.band32 = (float)ca.band;
+  for (int i = 0; i < 3; i++) { ca.lo32[i] = (float)c->lo[i]; ca.hi32[i] = (float)c->hi[i]; }
   const bool cull = c->n_obs <= kMaxCullObs;
 
   cudaError_t launch_err = cudaSuccess;
@@ -523,7 +532,8 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     using R = Robot<KIND>;
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
-      nn_mask<KIND><<<(unsigned)B, kNNThreads, 0, st>>>(rp, pv, nv, (float)opts->radius, opts->radius,
+      const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
+      nn_mask<KIND><<<(unsigned)B, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)opts->radius, opts->radius,
                                                        (float)ball_band, Ppad, P_<uint32_t>(c->mask),
                                                        P_<uint32_t>(c->cnt), ctr);
       nn_prefix<<<(P + 255) / 256, 256, 0, st>>>(P, (int)B, P_<uint32_t>(c->cnt), P_<uint32_t>(c->tot));

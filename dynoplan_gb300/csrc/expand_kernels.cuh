@@ -63,6 +63,7 @@ struct PrimView {
   const Pose<float> *pose32; // [PARTS][S] (3-D: cx,cy,c = position, s unused)
   const Pose<double> *pose64;
   const double *pbox;        // [P][2*POSD]: lo..., hi... of the state positions
+  const float *pbox32;       // the same, rounded outward
   const int64_t *coff;       // [P] first chunk row of primitive p
   const float *cbox32;       // [sum chunks][2*POSD]: centre..., half... of the parts'
                              //   bounding box over kChunk states (outward rounded)
@@ -130,21 +131,21 @@ __global__ void prep_nodes(NodeView nv) {
 // ------------------------------------------------------------ ball scan ---
 
 template <int KIND>
-__device__ __forceinline__ float key_dist32(const RobotParams &rp, const float *nk,
+__device__ __forceinline__ float key_dist32(const float4 w, const float *nk,
                                             const float *sk, int stride, float kc) {
   if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
-    return kc + (float)rp.w[1] * so2w(nk[0], sk[0]);
+    return kc + w.y * so2w(nk[0], sk[0]);
   } else if constexpr (KIND == DPG_ROBOT_CAR1) {
-    return kc + (float)rp.w[1] * so2w(nk[0], sk[0]) + (float)rp.w[2] * so2w(nk[1], sk[stride]);
+    return kc + w.y * so2w(nk[0], sk[0]) + w.z * so2w(nk[1], sk[stride]);
   } else if constexpr (KIND == DPG_ROBOT_QUAD2D) {
-    return kc + (float)rp.w[1] * so2w(nk[0], sk[0]) + (float)rp.w[3] * fabsf(nk[1] - sk[stride]);
+    return kc + w.y * so2w(nk[0], sk[0]) + w.w * fabsf(nk[1] - sk[stride]);
   } else {
     float dq = fabsf(nk[0] * sk[0] + nk[1] * sk[stride] + nk[2] * sk[2 * stride] +
                      nk[3] * sk[3 * stride]);
     dq = fminf(dq, 1.0f);
     const float a = nk[4] - sk[4 * stride], b = nk[5] - sk[5 * stride],
                 c = nk[6] - sk[6 * stride];
-    return kc + (float)rp.w[1] * acosf(dq) + (float)rp.w[3] * sqrtf(a * a + b * b + c * c);
+    return kc + w.y * acosf(dq) + w.w * sqrtf(a * a + b * b + c * c);
   }
 }
 
@@ -153,7 +154,7 @@ __device__ __forceinline__ float key_dist32(const RobotParams &rp, const float *
 // cnt[b * P + p] = members of prim p among the block's nodes.
 template <int KIND>
 __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView pv, NodeView nv,
-                                                      float radius, double radius64, float band, int Ppad,
+                                                      float4 w32, float radius, double radius64, float band, int Ppad,
                                                       uint32_t *mask, uint32_t *cnt,
                                                       DevCounters *ctr) {
   using R = Robot<KIND>;
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView p
         const int j = j0 + jj;
         bool in = false;
         if (live) {
-          const float d = key_dist32<KIND>(rp, nk, &sk[j], kNNTile, skc[j]);
+          const float d = key_dist32<KIND>(w32, nk, &sk[j], kNNTile, skc[j]);
           in = d <= radius;
           if (fabsf(d - radius) <= band) {  // decide in FP64
             const int p = p0 + j;
@@ -349,7 +350,7 @@ __global__ void build_poses(RobotParams rp, int64_t S, const double *st64, Pose<
 // swept position box of the canonical states.
 template <int KIND>
 __global__ void build_keys(RobotParams rp, int P, const int32_t *len, const int64_t *soff,
-                           const double *st64, float *key32, float *kconst32, double *pbox) {
+                           const double *st64, float *key32, float *kconst32, double *pbox, float *pbox32) {
   using R = Robot<KIND>;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
@@ -378,6 +379,8 @@ __global__ void build_keys(RobotParams rp, int P, const int32_t *len, const int6
   for (int i = 0; i < R::POSD; i++) {
     pbox[(int64_t)p * 2 * R::POSD + i] = lo[i];
     pbox[(int64_t)p * 2 * R::POSD + R::POSD + i] = hi[i];
+    pbox32[(int64_t)p * 2 * R::POSD + i] = __double2float_rd(lo[i]);
+    pbox32[(int64_t)p * 2 * R::POSD + R::POSD + i] = __double2float_ru(hi[i]);
   }
 }
 
