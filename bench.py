@@ -44,13 +44,13 @@ L2_FLUSH_BYTES = 512 << 20
 # DRAM bytes per check_pairs launch from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum), scaled to the full workload by checked pairs; None
 # until a capture exists.
-CHECK_TRAFFIC_PER_PAIR = None
+CHECK_TRAFFIC_PER_PAIR = 79.8e6 / 4126228  # profiles/check_pairs_car1_50k.md
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=2)
