@@ -44,7 +44,7 @@ L2_FLUSH_BYTES = 512 << 20
 # DRAM bytes per check_pairs launch from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum), scaled to the full workload by checked pairs; None
 # until a capture exists.
-CHECK_TRAFFIC_PER_PAIR = 79.8e6 / 4126228  # profiles/check_pairs_car1_50k.md
+CHECK_TRAFFIC_PER_PAIR = 79.8e6 / 4126228  # ncu capture of check_pairs, car1_v0 with 50,000 nodes
 
 
 def parse():

@@ -69,6 +69,8 @@ SIGNATURES = [
                                  C.c_void_p, C.c_void_p]),
     ("dpg_expand", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p,
                              C.POINTER(ExpandOut)]),
+    ("dpg_expand_noalloc", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p,
+                                     C.POINTER(ExpandOut)]),
     ("dpg_sync", C.c_int, [C.c_void_p]),
     ("dpg_set_abort", C.c_int, [C.c_void_p, C.c_int32]),
     ("dpg_host_alloc", C.c_void_p, [C.c_size_t]),

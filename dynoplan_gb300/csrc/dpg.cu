@@ -9,6 +9,7 @@
 #include <new>
 #include <numeric>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "dpg.h"
@@ -602,6 +603,214 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   cudaEventElapsedTime(&t_in, c->ev[0], c->ev[1]);
   cudaEventElapsedTime(&t_out, c->ev[4], c->ev[5]);
   c->timings[3] = t_in + t_out;
+  return DPG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free batched expand (dpg_expand_noalloc, declared in dpg.h).
+//
+// Who needs it: callers that must not allocate device memory at expand time
+// -- code that records the expand into a CUDA graph while a stream is being
+// captured (allocation calls are not allowed there), real-time planning loops
+// that cannot block on the device allocator, and hosts that hand all device
+// memory to their own pool.  dpg_expand may grow its per-context buffers with
+// cudaMalloc on any call; this entry point never does.
+//
+// Its per-call scratch (node keys and offsets, ball bitmask, per-tile counts,
+// segment bases, work-queue counters) lives in one file-scope device array of
+// kNoAllocScratchBytes.  Every GPU that loads this library holds that array
+// until the process exits.  All calls share it and it keeps the contents of
+// the last call: the counters are cleared at the start of every call, and
+// calls whose device work overlaps (two streams, two host threads) race on it.
+// The first call on a device looks the array's device address up with
+// cudaGetSymbolAddress (once per device, with that device current); make that
+// first call before any stream capture.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;  // 64 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// device address of g_noalloc_scratch on `device` (which must be current)
+int noalloc_scratch(dpg_ctx *c, int device, unsigned char **out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return fail(c, DPG_ERR_ARG, "noalloc: device index too large");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(c, DPG_ERR_CUDA, std::string("noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_addr[device] = p;
+  }
+  *out = static_cast<unsigned char *>(g_noalloc_addr[device]);
+  return DPG_OK;
+}
+
+size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+}  // namespace
+
+extern "C" {
+
+int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double *x_dev,
+                       dpg_expand_out *out) {
+  if (!c || !opts || !out) return DPG_ERR_ARG;
+  if (!c->have_prims || !c->have_env) return fail(c, DPG_ERR_STATE, "noalloc: upload primitives and env first");
+  if (N < 0 || (N > 0 && !x_dev)) return fail(c, DPG_ERR_ARG, "noalloc: bad node array");
+  if (!out->node || !out->prim)
+    return fail(c, DPG_ERR_ARG, "noalloc: the caller provides device arrays for node and prim");
+  if (!(opts->radius >= 0) || (opts->precision != DPG_FP32 && opts->precision != DPG_FP64))
+    return fail(c, DPG_ERR_ARG, "noalloc: bad radius or precision");
+  if (out->capacity < 0 || out->capacity > (int64_t)0xffffffffLL)
+    return fail(c, DPG_ERR_ARG, "noalloc: capacity out of range");
+  if (*(volatile int *)c->h_abort) return fail(c, DPG_ERR_ABORTED, "noalloc: abort flag raised");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const int kind = c->robot.kind, P = c->P;
+  const int kd = key_dim(kind), od = off_dim(kind);
+  const bool fp64 = opts->precision == DPG_FP64;
+  const int64_t cap = out->capacity;
+  const int Ppad = (P + 31) / 32 * 32;
+  const int64_t W = (N + 31) / 32;
+  const int64_t B = (N + kNNThreads - 1) / kNNThreads;
+
+  // carve the scratch; reject sizes beyond the array
+  size_t off_key = 0;
+  size_t off_off = off_key + align256(sizeof(float) * kd * (size_t)N);
+  size_t off_mask = off_off + align256(sizeof(float) * od * (size_t)N);
+  size_t off_cnt = off_mask + align256(sizeof(uint32_t) * (size_t)W * Ppad);
+  size_t off_tot = off_cnt + align256(sizeof(uint32_t) * (size_t)B * P);
+  size_t off_pbase = off_tot + align256(sizeof(uint32_t) * (size_t)P);
+  size_t off_opb = off_pbase + align256(sizeof(unsigned long long) * (size_t)P);
+  size_t off_oib = off_opb + align256(sizeof(unsigned long long) * ((size_t)P + 1));
+  size_t off_ctr = off_oib + align256(sizeof(unsigned long long) * ((size_t)P + 1));
+  const size_t need = off_ctr + align256(sizeof(DevCounters));
+  if (need > kNoAllocScratchBytes)
+    return fail(c, DPG_ERR_ARG, "noalloc: N x P too large for the " + std::to_string(kNoAllocScratchBytes >> 20) +
+                                    " MiB scratch (needs " + std::to_string(need >> 20) + " MiB)");
+  unsigned char *base = nullptr;
+  int rc;
+  if ((rc = noalloc_scratch(c, c->device, &base))) return rc;
+  float *nkey32 = reinterpret_cast<float *>(base + off_key);
+  float *noff32 = reinterpret_cast<float *>(base + off_off);
+  uint32_t *mask = reinterpret_cast<uint32_t *>(base + off_mask);
+  uint32_t *cnt = reinterpret_cast<uint32_t *>(base + off_cnt);
+  uint32_t *tot = reinterpret_cast<uint32_t *>(base + off_tot);
+  unsigned long long *pbase = reinterpret_cast<unsigned long long *>(base + off_pbase);
+  unsigned long long *ord_pbase = reinterpret_cast<unsigned long long *>(base + off_opb);
+  unsigned long long *ord_ibase = reinterpret_cast<unsigned long long *>(base + off_oib);
+  DevCounters *ctr = reinterpret_cast<DevCounters *>(base + off_ctr);
+
+  cudaStream_t st = c->stream;
+  CUDA_TRY(c, cudaMemsetAsync(ctr, 0, sizeof(DevCounters), st));  // counters start at zero
+
+  PrimView pv{};
+  pv.P = P;
+  pv.S = c->S;
+  pv.len = P_<int32_t>(c->len);
+  pv.soff = P_<int64_t>(c->soff);
+  pv.order = P_<int32_t>(c->order);
+  pv.key32 = P_<float>(c->key32);
+  pv.kconst32 = P_<float>(c->kconst32);
+  pv.st64 = P_<double>(c->st64);
+  pv.st32 = P_<float>(c->st32);
+  pv.pose32 = P_<Pose<float>>(c->pose32);
+  pv.pose64 = P_<Pose<double>>(c->pose64);
+  pv.pbox = P_<double>(c->pbox);
+  pv.pbox32 = P_<float>(c->pbox32);
+  pv.coff = P_<int64_t>(c->coff);
+  pv.cbox32 = P_<float>(c->cbox32);
+  pv.tbox32 = P_<float>(c->tbox32);
+  NodeView nv{N, x_dev, nkey32, noff32};
+  EnvView ev{};
+  ev.dim = c->dim;
+  for (int i = 0; i < 3; i++) { ev.lo[i] = c->lo[i]; ev.hi[i] = c->hi[i]; }
+  ev.n_obs = c->n_obs;
+  ev.obs32 = c->obs32.p;
+  ev.obs64 = c->obs64.p;
+  PairView po{};
+  po.cap = cap;
+  po.node = out->node;
+  po.prim = out->prim;
+  po.verdict = out->verdict;
+  po.first_invalid = out->first_invalid;
+  po.end_state = out->end_state;
+  po.min_gap = out->min_gap;
+  po.flags = out->flags;
+  const RobotParams rp = c->rp;
+  const double band = opts->contact_band > 0 ? opts->contact_band : 1e-4;
+  const double ball_band = opts->ball_band > 0 ? opts->ball_band : 1e-5;
+  CheckArgs ca{};
+  ca.rp = rp;
+  ca.pv = pv;
+  ca.nv = nv;
+  ca.ev = ev;
+  ca.out = po;
+  ca.ord_pbase = ord_pbase;
+  ca.ord_ibase = ord_ibase;
+  ca.ctr = ctr;
+  ca.abort_flag = c->d_abort;
+  ca.band = fp64 ? 0.0 : band;
+  ca.cull_margin = kGapCap + (float)band + 1e-3f;
+  ca.dt32 = (float)rp.dt;
+  ca.half_len32 = (float)rp.half_len;
+  ca.half_wid32 = (float)rp.half_wid;
+  ca.radius32 = (float)rp.radius;
+  ca.band32 = (float)ca.band;
+  for (int i = 0; i < 3; i++) { ca.lo32[i] = (float)c->lo[i]; ca.hi32[i] = (float)c->hi[i]; }
+  const bool cull = c->n_obs <= kMaxCullObs;
+
+  cudaError_t launch_err = cudaSuccess;
+  with_kind(kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    using R = Robot<KIND>;
+    if (N > 0) {
+      prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
+      const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
+      nn_mask<KIND><<<(unsigned)B, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)opts->radius, opts->radius,
+                                                       (float)ball_band, Ppad, mask, cnt, ctr);
+      nn_prefix<<<(P + 255) / 256, 256, 0, st>>>(P, (int)B, cnt, tot);
+    } else {
+      cudaMemsetAsync(tot, 0, sizeof(uint32_t) * P, st);
+    }
+    scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), tot, pbase, ord_pbase, ord_ibase, cap, ctr);
+    if (N > 0) {
+      dim3 eg((unsigned)((Ppad / 32 + 7) / 8), (unsigned)B);
+      nn_emit<<<eg, 256, 0, st>>>(P, Ppad, W, mask, cnt, pbase, cap, po.node, po.prim);
+    }
+    const size_t obs_bytes32 = R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>);
+    const size_t obs_bytes64 = R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>);
+    auto launch = [&](auto kern, size_t obs_bytes) {
+      const size_t sm = obs_bytes * std::max(c->n_obs, 1);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
+      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+    };
+    if (fp64) {
+      if (cull) launch(check_pairs<KIND, double, false, true>, obs_bytes64);
+      else launch(check_pairs<KIND, double, false, false>, obs_bytes64);
+    } else {
+      if (cull) launch(check_pairs<KIND, float, true, true>, obs_bytes32);
+      else launch(check_pairs<KIND, float, true, false>, obs_bytes32);
+    }
+    launch_err = cudaGetLastError();
+  });
+  if (launch_err != cudaSuccess)
+    return fail(c, DPG_ERR_CUDA, std::string("noalloc launch: ") + cudaGetErrorString(launch_err));
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_ctr, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  const DevCounters h = *c->h_ctr;
+  out->n_pairs = (int64_t)h.n_pairs;
+  out->n_scanned = N * (int64_t)P;
+  out->n_contact_recheck = (int64_t)h.n_recheck;
+  out->n_ball_recheck = (int64_t)h.n_ball_recheck;
+  if (h.status == DPG_ERR_ABORTED) return fail(c, DPG_ERR_ABORTED, "noalloc: aborted");
+  if ((int64_t)h.n_pairs > cap) return fail(c, DPG_ERR_CAPACITY, "noalloc: output capacity too small");
   return DPG_OK;
 }
 

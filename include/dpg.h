@@ -154,6 +154,30 @@ int dpg_upload_env(dpg_ctx *ctx, int32_t dim, const double *lo, const double *hi
 int dpg_expand(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x,
                dpg_expand_out *out);
 
+/* Allocation-free form of dpg_expand.  No counterpart in the reference (its
+ * expansion runs on the host).  For callers that cannot allocate device
+ * memory at expand time: code capturing a CUDA graph, real-time planning
+ * loops that must not block on the allocator, hosts that give all device
+ * memory to their own pool.  dpg_expand may call cudaMalloc to grow its
+ * buffers; this call never allocates: its per-call scratch is one 64 MiB
+ * file-scope device array that every GPU loading the library holds until
+ * exit.
+ *   - x_dev (N x nx doubles) and every array in `out` are DEVICE pointers;
+ *     out->node and out->prim are required.  opts->x_on_device and
+ *     opts->out_on_device are ignored (both are device).
+ *   - The scratch must hold 4*(KEYD+offset_dim)*N + 4*ceil(N/32)*ceil32(P)
+ *     + 4*ceil(N/256)*P + ~28*P bytes (rounded up per buffer); larger N x P is
+ *     rejected with DPG_ERR_ARG and a message.  About 60,000 car1 nodes x
+ *     5,000 primitives fit.
+ *   - All calls share the array, which keeps the last call's contents; the
+ *     call clears its counters itself.  Calls whose device work overlaps
+ *     (other streams or host threads) race on it: serialise them.
+ *   - The first call on a device looks the array up (cudaGetSymbolAddress);
+ *     make that first call before any stream capture.
+ * Results are identical to dpg_expand's with device outputs. */
+int dpg_expand_noalloc(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x_dev,
+                       dpg_expand_out *out);
+
 /* Wait for the context's stream. */
 int dpg_sync(dpg_ctx *ctx);
 /* Raise (1) or clear (0) the abort flag polled by the device work queue. */
