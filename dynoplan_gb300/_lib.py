@@ -76,6 +76,9 @@ SIGNATURES = [
     ("dpg_host_alloc", C.c_void_p, [C.c_size_t]),
     ("dpg_host_free", None, [C.c_void_p]),
     ("dpg_last_timings", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int32]),
+    # include/dpg_mlp.h
+    ("dpg_gemm_bf16", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                C.c_int]),
     # include/dpg_bench.h
     ("dpg_bench_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("dpg_bench_flush_l2", C.c_int, [C.c_int, C.c_size_t]),

@@ -1,0 +1,192 @@
+// gemm_kernels.cuh -- BF16 GEMM on the 5th-generation tensor cores (sm_103a).
+//
+//   C[M x N] = A[M x K] * B[N x K]^T      A, B bf16 row-major (K contiguous),
+//                                          FP32 accumulation in tensor memory
+//
+// One CTA of 128 threads computes a 128-row tile with every N column (N a
+// multiple of 16, <= 256) in one tcgen05.mma chain of M=128 x N x K=16
+// instructions; gridDim.y splits K.  K is consumed in chunks of 64 (one
+// 128-byte swizzle atom) staged into two shared-memory buffers: threads
+// stage chunk i+1 while the tensor cores run chunk i; an mbarrier that the
+// MMA commit arrives on tells the stagers when a buffer is free again.
+// Every wait is bounded: on expiry the kernel sets *err, drains, frees its
+// tensor memory and returns.  The epilogue reads one accumulator row per
+// thread (tcgen05.ld 32x32b) and hands 16 columns at a time to `Epi`.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "umma.cuh"
+
+namespace dpg {
+
+constexpr int kGemmThreads = 128;
+constexpr int kGemmKChunk = 64;
+
+__host__ __device__ constexpr int tmem_cols_for(int n) {
+  return n <= 32 ? 32 : (n <= 64 ? 64 : (n <= 128 ? 128 : 256));
+}
+__host__ __device__ constexpr size_t gemm_smem_bytes(int N) {
+  // two stages of (A 128x64 + B Nx64) bf16, 1024-aligned, + barriers + slack
+  return 2 * (size_t)(128 * 128 + N * 128) + 1024 + 64;
+}
+
+template <int N, class Epi>
+__global__ void __launch_bounds__(kGemmThreads) gemm_bf16_tn(const __nv_bfloat16 *__restrict__ A,
+                                                              const __nv_bfloat16 *__restrict__ B, int M,
+                                                              int K, int k_per_split, Epi epi, int *err) {
+  static_assert(N % 16 == 0 && N >= 16 && N <= 256, "N");
+  extern __shared__ unsigned char smem_raw[];
+  // 1024-byte aligned stage buffers
+  const uint32_t raw = umma::smem_u32(smem_raw);
+  unsigned char *base = smem_raw + ((1024 - (raw & 1023)) & 1023);
+  constexpr int kA = 128 * 128, kB = N * 128;
+  unsigned char *tileA[2] = {base, base + kA + kB};
+  unsigned char *tileB[2] = {base + kA, base + 2 * kA + kB};
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(base + 2 * (kA + kB));
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+  __shared__ int s_bad;
+
+  const int m0 = blockIdx.x * 128;
+  const int kbeg = blockIdx.y * k_per_split;
+  const int kend = min(K, kbeg + k_per_split);
+  const int nchunks = (kend - kbeg) / kGemmKChunk;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr uint32_t kCols = tmem_cols_for(N);
+  constexpr uint32_t idesc = umma::idesc_bf16_f32(128, N);
+
+  if (threadIdx.x == 0) {
+    umma::mbar_init(&mbar[0], 1);
+    umma::mbar_init(&mbar[1], 1);
+    umma::mbar_fence_init();
+    s_bad = 0;
+  }
+  if (warp == 0) {
+    umma::tmem_alloc(tslot, kCols);
+    umma::tmem_relinquish();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const int rows_valid = min(128, M - m0);
+
+  bool bad = false;
+  int issued = 0;  // chunks whose MMAs were issued (identical in every thread)
+  for (int i = 0; i < nchunks && !bad; i++) {
+    const int s = i & 1;
+    if (i >= 2) {  // buffer s is free once the MMAs of chunk i-2 are done
+      bool ok = umma::mbar_wait(&mbar[s], ((i - 2) >> 1) & 1);
+      if (__syncthreads_or(!ok)) { bad = true; break; }
+    }
+    const int k0 = kbeg + i * kGemmKChunk;
+    umma::stage_kmajor(tileA[s], A + (int64_t)m0 * K, K, 128, rows_valid, k0, 1);
+    umma::stage_kmajor(tileB[s], B, K, N, N, k0, 1);
+    umma::fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      umma::fence_after_sync();
+      const uint32_t a0 = umma::smem_u32(tileA[s]), b0 = umma::smem_u32(tileB[s]);
+#pragma unroll
+      for (int kk = 0; kk < kGemmKChunk / 16; kk++)
+        umma::mma_bf16(tmem, umma::sdesc_kmajor_sw128(a0 + kk * 32), umma::sdesc_kmajor_sw128(b0 + kk * 32),
+                       idesc, (i > 0 || kk > 0) ? 1u : 0u);
+      umma::commit(&mbar[s]);
+    }
+    issued = i + 1;
+  }
+  if (!bad && nchunks > 0) {  // all MMAs done
+    const int last = nchunks - 1;
+    bool ok = umma::mbar_wait(&mbar[last & 1], (last >> 1) & 1);
+    bad = __syncthreads_or(!ok);
+  }
+  if (bad) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    // let in-flight MMAs finish before the tensor memory is released
+    if (issued > 0) umma::mbar_wait(&mbar[(issued - 1) & 1], ((issued - 1) >> 1) & 1, 1u << 20);
+  } else if (nchunks > 0) {
+    umma::fence_after_sync();
+    const int row = 32 * warp + lane;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      float v[16];
+      umma::tmem_ld16(lane_addr + c0, v);
+      if (m0 + row < M) epi(m0 + row, c0, v);
+    }
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, kCols);
+}
+
+// ---- epilogues ---------------------------------------------------------------
+struct EpiStoreF32 {  // C = acc (ldc = row stride, only columns < n_valid)
+  float *C;
+  int ldc, n_valid;
+  __device__ void operator()(int row, int c0, const float *v) const {
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+      if (c0 + j < n_valid) C[(int64_t)row * ldc + c0 + j] = v[j];
+  }
+};
+struct EpiAtomicF32 {  // C += acc (split-K partial sums)
+  float *C;
+  int ldc, n_valid;
+  __device__ void operator()(int row, int c0, const float *v) const {
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+      if (c0 + j < n_valid) atomicAdd(C + (int64_t)row * ldc + c0 + j, v[j]);
+  }
+};
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float z) {
+  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * __expf(-0.5f * z * z);
+  return cdf + z * pdf;
+}
+
+// z = acc + bias; keeps z (FP32, for the backward pass) when pre != nullptr;
+// writes gelu(z) in bf16
+struct EpiBiasGelu {
+  const float *bias;
+  float *pre;
+  __nv_bfloat16 *act;
+  int ld;
+  __device__ void operator()(int row, int c0, const float *v) const {
+    __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const float z = v[j] + bias[c0 + j];
+      if (pre) pre[(int64_t)row * ld + c0 + j] = z;
+      h[j] = __float2bfloat16_rn(gelu(z));
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(act + (int64_t)row * ld + c0);
+    dst[0] = reinterpret_cast<const uint4 *>(h)[0];
+    dst[1] = reinterpret_cast<const uint4 *>(h)[1];
+  }
+};
+// out = acc + bias (FP32), first n_valid columns
+struct EpiBias {
+  const float *bias;
+  float *out;
+  int ld, n_valid;
+  __device__ void operator()(int row, int c0, const float *v) const {
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+      if (c0 + j < n_valid) out[(int64_t)row * ld + c0 + j] = v[j] + bias[c0 + j];
+  }
+};
+
+// ---- SIMT reference (CUDA cores, FP32 accumulation) ---------------------------
+__global__ void gemm_bf16_ref(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *C, int M, int N, int K) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)M * N) return;
+  const int m = (int)(i / N), n = (int)(i % N);
+  float s = 0.f;
+  for (int k = 0; k < K; k++) s += __bfloat162float(A[(int64_t)m * K + k]) * __bfloat162float(B[(int64_t)n * K + k]);
+  C[i] = s;
+}
+
+}  // namespace dpg

@@ -1,0 +1,147 @@
+// umma.cuh -- 5th-generation tensor-core (tcgen05) building blocks for sm_103a,
+// written as inline PTX: tensor-memory allocation, shared-memory matrix
+// descriptors, the BF16 x BF16 -> FP32 MMA, commit to an mbarrier, and
+// tensor-memory loads.  Used by the surrogate-MLP kernels (mlp_kernels.cuh).
+//
+// Operand layout used throughout: K-major with the 128-byte swizzle.  A tile
+// of R rows x K bf16 is stored as K/64 "k-blocks" of R x 128 bytes; inside a
+// k-block row r occupies bytes (r/8)*1024 + (r%8)*128 and its 16-byte chunk c
+// sits at chunk (c ^ (r%8)).  Tiles start on 1024-byte boundaries.
+#pragma once
+
+#include <cstdint>
+#include <cuda_bf16.h>
+
+namespace dpg {
+namespace umma {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ---- tensor memory -------------------------------------------------------
+// One full warp allocates `ncols` (power of two, >= 32) columns x 128 lanes
+// of 32-bit tensor memory; the base address is written to *dst (shared).
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// generic-proxy shared-memory writes become visible to the tensor cores
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---- mbarrier -------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after `limit` polls and returns false (the caller
+// records an error and winds down instead of spinning forever).
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, uint32_t limit = 1u << 22) {
+  for (uint32_t i = 0; i < limit; i++)
+    if (mbar_try_wait(b, parity)) return true;
+  return false;
+}
+
+// ---- descriptors -----------------------------------------------------------
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);   // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
+  d |= (uint64_t)1 << 46;                    // version
+  d |= (uint64_t)2 << 61;                    // 128-byte swizzle
+  return d;
+}
+// Instruction descriptor of kind::f16: BF16 A and B (K-major), FP32 D, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+  return (1u << 4)                       // D format F32
+         | (1u << 7)                     // A format BF16
+         | (1u << 10)                    // B format BF16
+         | ((uint32_t)(N >> 3) << 17)    // N / 8
+         | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// ---- MMA --------------------------------------------------------------------
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// the mbarrier receives one arrive once every MMA this thread issued is done
+__device__ __forceinline__ void commit(uint64_t *b) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(b))
+               : "memory");
+}
+
+// ---- tensor memory -> registers ---------------------------------------------
+// 32 lanes x 16 consecutive 32-bit columns: thread t of the warp gets lane
+// (lane_base + t), columns col..col+15.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- operand staging -----------------------------------------------------------
+// byte offset of (row r, 16-byte chunk g) in a K-major SW128 tile of R rows
+__device__ __forceinline__ uint32_t kmajor_offset(int R, int r, int g) {
+  const int kb = g >> 3, c = g & 7;
+  return (uint32_t)kb * (uint32_t)R * 128u + (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u +
+         (uint32_t)((c ^ (r & 7)) << 4);
+}
+
+// Copy rows [0, R) x bf16 columns [k0, k0 + 64*KB) of a row-major global
+// matrix (leading dimension ld elements) into a K-major SW128 tile; rows at
+// or beyond `rows_valid` are zero-filled.  All threads of the block help.
+__device__ __forceinline__ void stage_kmajor(unsigned char *tile, const __nv_bfloat16 *g, int64_t ld, int R,
+                                             int rows_valid, int k0, int KB) {
+  const int chunks = R * KB * 8;
+  for (int i = threadIdx.x; i < chunks; i += blockDim.x) {
+    const int r = i / (KB * 8), gch = i % (KB * 8);
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (r < rows_valid) v = *reinterpret_cast<const uint4 *>(g + (int64_t)r * ld + k0 + gch * 8);
+    *reinterpret_cast<uint4 *>(tile + kmajor_offset(R, r, gch)) = v;
+  }
+}
+
+}  // namespace umma
+}  // namespace dpg
