@@ -79,6 +79,16 @@ SIGNATURES = [
     # include/dpg_mlp.h
     ("dpg_gemm_bf16", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                 C.c_int]),
+    ("dpg_mlp_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int64, C.c_uint64]),
+    ("dpg_mlp_destroy", None, [C.c_void_p]),
+    ("dpg_mlp_param_size", C.c_int64, [C.c_void_p, C.c_int]),
+    ("dpg_mlp_get", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    ("dpg_mlp_set", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    ("dpg_mlp_node_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("dpg_mlp_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("dpg_mlp_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                     C.c_float, C.c_float, C.POINTER(C.c_float)]),
+    ("dpg_mlp_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     # include/dpg_bench.h
     ("dpg_bench_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("dpg_bench_flush_l2", C.c_int, [C.c_int, C.c_size_t]),

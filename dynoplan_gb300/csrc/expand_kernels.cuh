@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView p
 }
 
 // per primitive: cnt[b][p] -> exclusive prefix over b; tot[p] = total
-__global__ void nn_prefix(int P, int B, uint32_t *cnt, uint32_t *tot) {
+static __global__ void nn_prefix(int P, int B, uint32_t *cnt, uint32_t *tot) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   uint32_t run = 0;
@@ -230,7 +230,7 @@ __global__ void nn_prefix(int P, int B, uint32_t *cnt, uint32_t *tot) {
 
 // Single block: bases of each primitive's pair segment and of its work
 // items, in the order of decreasing primitive length.
-__global__ void __launch_bounds__(1024) scan_totals(int P, const int32_t *order, const uint32_t *tot,
+static __global__ void __launch_bounds__(1024) scan_totals(int P, const int32_t *order, const uint32_t *tot,
                                                     unsigned long long *pbase,
                                                     unsigned long long *ord_pbase,
                                                     unsigned long long *ord_ibase, int64_t cap,
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(1024) scan_totals(int P, const int32_t *order,
 }
 
 // Warp per (node tile b, 32 primitives); lane = primitive.
-__global__ void __launch_bounds__(256) nn_emit(int P, int Ppad, int64_t W, const uint32_t *mask,
+static __global__ void __launch_bounds__(256) nn_emit(int P, int Ppad, int64_t W, const uint32_t *mask,
                                                const uint32_t *loc, const unsigned long long *pbase,
                                                int64_t cap, uint32_t *pair_node, uint32_t *pair_prim) {
   const int lane = threadIdx.x & 31;

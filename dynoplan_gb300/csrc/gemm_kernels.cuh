@@ -180,7 +180,7 @@ struct EpiBias {
 };
 
 // ---- SIMT reference (CUDA cores, FP32 accumulation) ---------------------------
-__global__ void gemm_bf16_ref(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *C, int M, int N, int K) {
+static __global__ void gemm_bf16_ref(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *C, int M, int N, int K) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)M * N) return;
   const int m = (int)(i / N), n = (int)(i % N);

@@ -74,3 +74,329 @@ extern "C" int dpg_gemm_bf16(const void *A_dev, const void *B_dev, float *C_dev,
   cudaMemcpy(&h, g_err, sizeof(int), cudaMemcpyDeviceToHost);
   return h ? DPG_ERR_TIMEOUT : DPG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// The surrogate MLP (include/dpg_mlp.h).
+#include <cmath>
+#include <vector>
+
+#include "mlp_kernels.cuh"
+
+struct dpg_mlp {
+  int device = 0;
+  int P = 0;
+  int64_t max_rows = 0, rows_pad = 0;
+  cudaStream_t stream = nullptr;
+  // FP32 master parameters, gradients, Adam moments
+  float *w[DPG_MLP_NPARAM] = {}, *g[DPG_MLP_NPARAM] = {}, *m[DPG_MLP_NPARAM] = {}, *v[DPG_MLP_NPARAM] = {};
+  int64_t n[DPG_MLP_NPARAM] = {};
+  // bf16 operands: W16[l] [out x in], WT16[l] its transpose (layer 4 padded
+  // to K = 64), emb16 the embedding table
+  __nv_bfloat16 *W16[4] = {}, *WT16[4] = {}, *emb16 = nullptr;
+  // activations and backward buffers (rows_pad rows)
+  __nv_bfloat16 *X = nullptr, *H[3] = {}, *dZa = nullptr, *dZb = nullptr, *dY = nullptr, *T1 = nullptr,
+                *T2 = nullptr;
+  float *Z[3] = {}, *out = nullptr, *loss = nullptr;
+  int *err = nullptr;
+  int step = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double last_ms = 0, last_flops = 0;
+};
+
+namespace {
+
+constexpr int kIn[4] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden};
+constexpr int kOut[4] = {kMlpHidden, kMlpHidden, kMlpHidden, kMlpOutPad};
+constexpr int kDY = 64;  // loss-gradient row width (K of the dH3 GEMM)
+
+__global__ void init_normal(float *w, int64_t n, float stdev, uint64_t seed, int rows_valid, int cols) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  auto mix = [](uint64_t x) {
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+  };
+  const uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
+  const uint64_t a = mix(z), b = mix(z ^ 0xD1B54A32D192ED03ull);
+  const float u1 = (float)(((a >> 11) + 1) * (1.0 / 9007199254740993.0));
+  const float u2 = (float)((b >> 11) * (1.0 / 9007199254740992.0));
+  const float r = sqrtf(-2.f * logf(u1)) * cosf(6.2831853f * u2);
+  w[i] = (i / cols < rows_valid) ? stdev * r : 0.f;
+}
+
+int64_t pad128(int64_t n) { return (n + 127) / 128 * 128; }
+
+// bf16 copy of parameter `which` (and, for weights, the transpose)
+void refresh_bf16(dpg_mlp *M, int which, cudaStream_t st) {
+  const int64_t n = M->n[which];
+  if (which == DPG_MLP_EMB) {
+    f32_to_bf16<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(M->w[which], M->emb16, n);
+    return;
+  }
+  if (which % 2) return;  // biases stay FP32
+  const int l = which / 2, rows = kOut[l], cols = kIn[l];
+  f32_to_bf16<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(M->w[which], M->W16[l], n);
+  dim3 tb(32, 8), tg((cols + 31) / 32, (rows + 31) / 32);
+  if (l < 3) {
+    transpose_bf16<<<tg, tb, 0, st>>>(M->W16[l], M->WT16[l], rows, cols);
+  } else {  // [16 x 256] -> [256 x 16] -> rows of 64 (zero padded)
+    transpose_bf16<<<tg, tb, 0, st>>>(M->W16[l], M->T1, rows, cols);
+    cudaMemsetAsync(M->WT16[3], 0, sizeof(__nv_bfloat16) * kMlpHidden * kDY, st);
+    cudaMemcpy2DAsync(M->WT16[3], kDY * sizeof(__nv_bfloat16), M->T1, kMlpOutPad * sizeof(__nv_bfloat16),
+                      kMlpOutPad * sizeof(__nv_bfloat16), kMlpHidden, cudaMemcpyDeviceToDevice, st);
+  }
+}
+
+template <class T> cudaError_t dalloc(T **p, size_t count) {
+  return cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(count, 1));
+}
+
+// forward of rows [0, B) of the assembled X; keeps Z (FP32) when train
+cudaError_t forward_rows(dpg_mlp *M, int64_t B, bool train, float *out, cudaStream_t st) {
+  const int64_t Bp = pad128(B);
+  cudaError_t e;
+  const __nv_bfloat16 *in = M->X;
+  for (int l = 0; l < 3; l++) {
+    EpiBiasGelu epi{M->w[2 * l + 1], train ? M->Z[l] : nullptr, M->H[l], kMlpHidden};
+    e = launch_gemm(kMlpHidden, in, M->W16[l], (int)Bp, kIn[l], 1, epi, M->err, st);
+    if (e != cudaSuccess) return e;
+    in = M->H[l];
+  }
+  return launch_gemm(kMlpOutPad, M->H[2], M->W16[3], (int)Bp, kMlpHidden, 1, EpiBias{M->w[DPG_MLP_B4], out, 2, 2},
+                     M->err, st);
+}
+
+double forward_flops(int64_t Bp) {
+  return 2.0 * Bp * ((double)kMlpIn * kMlpHidden + 2.0 * kMlpHidden * kMlpHidden + kMlpHidden * kMlpOutPad);
+}
+
+int check_err(dpg_mlp *M) {
+  int h = 0;
+  cudaMemcpy(&h, M->err, sizeof(int), cudaMemcpyDeviceToHost);
+  return h ? DPG_ERR_TIMEOUT : DPG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dpg_mlp_create(dpg_mlp **out, int device, int n_prims, int64_t max_rows, uint64_t seed) {
+  if (!out || n_prims <= 0 || max_rows <= 0 || max_rows > ((int64_t)1 << 31) - 128) return DPG_ERR_ARG;
+  *out = nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return DPG_ERR_NODEVICE;
+  dpg_mlp *M = new dpg_mlp();
+  M->device = device;
+  M->P = n_prims;
+  M->max_rows = max_rows;
+  M->rows_pad = pad128(max_rows);
+  const int64_t R = M->rows_pad;
+  const int64_t sizes[DPG_MLP_NPARAM] = {(int64_t)kMlpHidden * kMlpIn, kMlpHidden, (int64_t)kMlpHidden * kMlpHidden,
+                                         kMlpHidden, (int64_t)kMlpHidden * kMlpHidden, kMlpHidden,
+                                         (int64_t)kMlpOutPad * kMlpHidden, kMlpOutPad, (int64_t)n_prims * kMlpEmb};
+  bool ok = cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking) == cudaSuccess;
+  for (int i = 0; i < DPG_MLP_NPARAM && ok; i++) {
+    M->n[i] = sizes[i];
+    ok = dalloc(&M->w[i], sizes[i]) == cudaSuccess && dalloc(&M->g[i], sizes[i]) == cudaSuccess &&
+         dalloc(&M->m[i], sizes[i]) == cudaSuccess && dalloc(&M->v[i], sizes[i]) == cudaSuccess;
+  }
+  for (int l = 0; l < 4 && ok; l++)
+    ok = dalloc(&M->W16[l], (size_t)kOut[l] * kIn[l]) == cudaSuccess &&
+         dalloc(&M->WT16[l], l < 3 ? (size_t)kOut[l] * kIn[l] : (size_t)kMlpHidden * kDY) == cudaSuccess;
+  ok = ok && dalloc(&M->emb16, (size_t)n_prims * kMlpEmb) == cudaSuccess &&
+       dalloc(&M->X, (size_t)R * kMlpIn) == cudaSuccess && dalloc(&M->dZa, (size_t)R * kMlpHidden) == cudaSuccess &&
+       dalloc(&M->dZb, (size_t)R * kMlpHidden) == cudaSuccess && dalloc(&M->dY, (size_t)R * kDY) == cudaSuccess &&
+       dalloc(&M->T1, (size_t)R * kMlpHidden) == cudaSuccess && dalloc(&M->T2, (size_t)R * kMlpHidden) == cudaSuccess &&
+       dalloc(&M->out, (size_t)R * 2) == cudaSuccess && dalloc(&M->loss, 1) == cudaSuccess &&
+       dalloc(&M->err, 1) == cudaSuccess;
+  for (int l = 0; l < 3 && ok; l++)
+    ok = dalloc(&M->H[l], (size_t)R * kMlpHidden) == cudaSuccess && dalloc(&M->Z[l], (size_t)R * kMlpHidden) == cudaSuccess;
+  ok = ok && cudaEventCreate(&M->e0) == cudaSuccess && cudaEventCreate(&M->e1) == cudaSuccess;
+  if (!ok) {
+    dpg_mlp_destroy(M);
+    return DPG_ERR_OOM;
+  }
+  cudaStream_t st = M->stream;
+  cudaMemsetAsync(M->err, 0, sizeof(int), st);
+  const float stdv[DPG_MLP_NPARAM] = {1.f / sqrtf(96.f), 0, 1.f / 16.f, 0, 1.f / 16.f, 0, 1.f / 16.f, 0, 0.5f};
+  for (int i = 0; i < DPG_MLP_NPARAM; i++) {
+    const int64_t n = M->n[i];
+    const int cols = (i == DPG_MLP_EMB) ? kMlpEmb : ((i % 2 == 0) ? kIn[i / 2] : (int)n);
+    const int rows_valid = (i == DPG_MLP_W4) ? 2 : (int)(n / cols);
+    if (stdv[i] > 0)
+      init_normal<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(M->w[i], n, stdv[i], seed + 7919ull * (i + 1),
+                                                               rows_valid, cols);
+    else
+      cudaMemsetAsync(M->w[i], 0, sizeof(float) * n, st);
+    cudaMemsetAsync(M->m[i], 0, sizeof(float) * n, st);
+    cudaMemsetAsync(M->v[i], 0, sizeof(float) * n, st);
+    cudaMemsetAsync(M->g[i], 0, sizeof(float) * n, st);
+  }
+  for (int i = 0; i < DPG_MLP_NPARAM; i++) refresh_bf16(M, i, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) {
+    dpg_mlp_destroy(M);
+    return DPG_ERR_CUDA;
+  }
+  *out = M;
+  return DPG_OK;
+}
+
+void dpg_mlp_destroy(dpg_mlp *M) {
+  if (!M) return;
+  cudaSetDevice(M->device);
+  if (M->stream) cudaStreamSynchronize(M->stream);
+  for (int i = 0; i < DPG_MLP_NPARAM; i++) {
+    cudaFree(M->w[i]);
+    cudaFree(M->g[i]);
+    cudaFree(M->m[i]);
+    cudaFree(M->v[i]);
+  }
+  for (int l = 0; l < 4; l++) {
+    cudaFree(M->W16[l]);
+    cudaFree(M->WT16[l]);
+  }
+  for (int l = 0; l < 3; l++) {
+    cudaFree(M->H[l]);
+    cudaFree(M->Z[l]);
+  }
+  void *bufs[] = {M->emb16, M->X, M->dZa, M->dZb, M->dY, M->T1, M->T2, M->out, M->loss, M->err};
+  for (void *b : bufs) cudaFree(b);
+  if (M->e0) cudaEventDestroy(M->e0);
+  if (M->e1) cudaEventDestroy(M->e1);
+  if (M->stream) cudaStreamDestroy(M->stream);
+  delete M;
+}
+
+int64_t dpg_mlp_param_size(const dpg_mlp *M, int which) {
+  return (M && which >= 0 && which < DPG_MLP_NPARAM) ? M->n[which] : -1;
+}
+
+int dpg_mlp_get(const dpg_mlp *M, int which, int grad, float *host) {
+  if (!M || !host || which < 0 || which >= DPG_MLP_NPARAM) return DPG_ERR_ARG;
+  cudaSetDevice(M->device);
+  cudaStreamSynchronize(M->stream);
+  return cudaMemcpy(host, grad ? M->g[which] : M->w[which], sizeof(float) * M->n[which], cudaMemcpyDeviceToHost) ==
+                 cudaSuccess
+             ? DPG_OK
+             : DPG_ERR_CUDA;
+}
+
+int dpg_mlp_set(dpg_mlp *M, int which, const float *host) {
+  if (!M || !host || which < 0 || which >= DPG_MLP_NPARAM) return DPG_ERR_ARG;
+  cudaSetDevice(M->device);
+  if (cudaMemcpyAsync(M->w[which], host, sizeof(float) * M->n[which], cudaMemcpyHostToDevice, M->stream) != cudaSuccess)
+    return DPG_ERR_CUDA;
+  refresh_bf16(M, which, M->stream);
+  return cudaStreamSynchronize(M->stream) == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+int dpg_mlp_forward(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_dev, const uint32_t *prim_dev,
+                    int64_t n, float *out_dev) {
+  if (!M || !node_feat_dev || !node_dev || !prim_dev || !out_dev || n < 0) return DPG_ERR_ARG;
+  cudaSetDevice(M->device);
+  cudaStream_t st = M->stream;
+  const auto *nf = static_cast<const __nv_bfloat16 *>(node_feat_dev);
+  cudaMemsetAsync(M->err, 0, sizeof(int), st);
+  cudaEventRecord(M->e0, st);
+  double flops = 0;
+  for (int64_t r0 = 0; r0 < n; r0 += M->max_rows) {
+    const int64_t B = std::min(M->max_rows, n - r0), Bp = pad128(B);
+    const int64_t chunks = Bp * (kMlpIn / 8);
+    mlp_assemble<<<(unsigned)((chunks + 255) / 256), 256, 0, st>>>(nf, M->emb16, node_dev + r0, prim_dev + r0, B, Bp,
+                                                                    M->X);
+    if (forward_rows(M, B, false, out_dev + 2 * r0, st) != cudaSuccess) return DPG_ERR_CUDA;
+    flops += forward_flops(Bp);
+  }
+  cudaEventRecord(M->e1, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return DPG_ERR_CUDA;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, M->e0, M->e1);
+  M->last_ms = ms;
+  M->last_flops = flops;
+  return check_err(M);
+}
+
+int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_dev, const uint32_t *prim_dev,
+                       const float *target_dev, int64_t B, float lr, float ctg_weight, float *loss) {
+  if (!M || !node_feat_dev || !node_dev || !prim_dev || !target_dev || B <= 0 || B > M->max_rows) return DPG_ERR_ARG;
+  cudaSetDevice(M->device);
+  cudaStream_t st = M->stream;
+  const int64_t Bp = pad128(B);
+  const int split = (int)std::max<int64_t>(1, std::min<int64_t>(64, Bp / 1024));
+  cudaMemsetAsync(M->err, 0, sizeof(int), st);
+  cudaMemsetAsync(M->loss, 0, sizeof(float), st);
+  for (int i = 0; i < DPG_MLP_NPARAM; i++) cudaMemsetAsync(M->g[i], 0, sizeof(float) * M->n[i], st);
+  cudaEventRecord(M->e0, st);
+  const auto *nf = static_cast<const __nv_bfloat16 *>(node_feat_dev);
+  const int64_t chunks = Bp * (kMlpIn / 8);
+  mlp_assemble<<<(unsigned)((chunks + 255) / 256), 256, 0, st>>>(nf, M->emb16, node_dev, prim_dev, B, Bp, M->X);
+  if (forward_rows(M, B, true, M->out, st) != cudaSuccess) return DPG_ERR_CUDA;
+  mlp_loss<<<(unsigned)((Bp + 255) / 256), 256, 0, st>>>(M->out, target_dev, B, Bp, ctg_weight, M->dY, M->loss);
+  dim3 tb(32, 8);
+  auto transpose = [&](const __nv_bfloat16 *in, __nv_bfloat16 *o, int64_t rows, int64_t cols) {
+    dim3 tg((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+    transpose_bf16<<<tg, tb, 0, st>>>(in, o, rows, cols);
+  };
+  auto colsum = [&](const __nv_bfloat16 *in, int ld, int ncol, float *o) {
+    dim3 g((ncol + 31) / 32, 64), b(32, 8);
+    column_sums_bf16<<<g, b, 0, st>>>(in, Bp, ld, ncol, o);
+  };
+  cudaError_t e = cudaSuccess;
+  // layer 4: dW4 = dY^T H3 (16 rows), db4, dZ3 = (dY W4) * gelu'(Z3)
+  transpose(M->dY, M->T1, Bp, kDY);
+  transpose(M->H[2], M->T2, Bp, kMlpHidden);
+  e = launch_gemm(kMlpHidden, M->T1, M->T2, kMlpOutPad, (int)Bp, split,
+                  EpiAtomicF32{M->g[DPG_MLP_W4], kMlpHidden, kMlpHidden}, M->err, st);
+  colsum(M->dY, kDY, kMlpOutPad, M->g[DPG_MLP_B4]);
+  if (e == cudaSuccess)
+    e = launch_gemm(kMlpHidden, M->dY, M->WT16[3], (int)Bp, kDY, 1, EpiGeluGrad{M->Z[2], M->dZa, kMlpHidden},
+                    M->err, st);
+  __nv_bfloat16 *dz = M->dZa, *dz_next = M->dZb;
+  for (int l = 2; l >= 0 && e == cudaSuccess; l--) {  // layers 3, 2, 1
+    const __nv_bfloat16 *h_in = l > 0 ? M->H[l - 1] : M->X;
+    transpose(dz, M->T1, Bp, kMlpHidden);
+    transpose(h_in, M->T2, Bp, kIn[l]);
+    e = launch_gemm(kIn[l], M->T1, M->T2, kMlpHidden, (int)Bp, split,
+                    EpiAtomicF32{M->g[2 * l], kIn[l], kIn[l]}, M->err, st);
+    colsum(dz, kMlpHidden, kMlpHidden, M->g[2 * l + 1]);
+    if (e != cudaSuccess) break;
+    if (l > 0)
+      e = launch_gemm(kMlpHidden, dz, M->WT16[l], (int)Bp, kMlpHidden, 1,
+                      EpiGeluGrad{M->Z[l - 1], dz_next, kMlpHidden}, M->err, st);
+    else
+      e = launch_gemm(kMlpIn, dz, M->WT16[0], (int)Bp, kMlpHidden, 1, EpiEmbGrad{prim_dev, M->g[DPG_MLP_EMB], B},
+                      M->err, st);
+    std::swap(dz, dz_next);
+  }
+  if (e != cudaSuccess) return DPG_ERR_CUDA;
+  // Adam
+  M->step++;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float bc1 = 1.f - powf(b1, (float)M->step), bc2 = 1.f - powf(b2, (float)M->step);
+  for (int i = 0; i < DPG_MLP_NPARAM; i++) {
+    const int64_t n = M->n[i];
+    adam_update<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(M->w[i], M->g[i], M->m[i], M->v[i], n, lr, b1, b2,
+                                                             eps, bc1, bc2, nullptr, nullptr, 0, 1);
+    refresh_bf16(M, i, st);
+  }
+  cudaEventRecord(M->e1, st);
+  float hl = 0;
+  cudaMemcpyAsync(&hl, M->loss, sizeof(float), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return DPG_ERR_CUDA;
+  if (loss) *loss = hl / (float)B;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, M->e0, M->e1);
+  M->last_ms = ms;
+  // forward + the two backward GEMMs per layer
+  M->last_flops = 3.0 * forward_flops(Bp);
+  return check_err(M);
+}
+
+int dpg_mlp_last_timing(const dpg_mlp *M, double *ms, double *flops) {
+  if (!M) return DPG_ERR_ARG;
+  if (ms) *ms = M->last_ms;
+  if (flops) *flops = M->last_flops;
+  return DPG_OK;
+}
+
+}  // extern "C"

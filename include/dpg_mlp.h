@@ -31,6 +31,44 @@ extern "C" {
 int dpg_gemm_bf16(const void *A_dev, const void *B_dev, float *C_dev, int M, int N, int K, int impl,
                   int split_k);
 
+/* ---- the surrogate MLP --------------------------------------------------
+ * Input row per (node, primitive) pair (96 bf16): normalised node state (16,
+ * zero padded), 8x8 occupancy patch around the node (64), the primitive's
+ * learned 16-D embedding.  Layers 96 -> 256 -> 256 -> 256 -> 2 with GELU;
+ * outputs [collision logit, cost-to-go].  BF16 weights and activations, FP32
+ * accumulation (tcgen05), FP32 master weights, Adam. */
+typedef struct dpg_mlp dpg_mlp;
+
+enum { DPG_MLP_W1 = 0, DPG_MLP_B1, DPG_MLP_W2, DPG_MLP_B2, DPG_MLP_W3, DPG_MLP_B3, DPG_MLP_W4, DPG_MLP_B4,
+       DPG_MLP_EMB, DPG_MLP_NPARAM };
+
+/* n_prims embedding rows; max_rows = largest batch of pairs per call */
+int dpg_mlp_create(dpg_mlp **mlp, int device, int n_prims, int64_t max_rows, uint64_t seed);
+void dpg_mlp_destroy(dpg_mlp *mlp);
+/* element count of parameter `which` (W1 256x96, W2/W3 256x256, W4 16x256
+ * with rows >= 2 held at zero, b1-b3 256, b4 16, EMB n_prims x 16) */
+int64_t dpg_mlp_param_size(const dpg_mlp *mlp, int which);
+/* host copies of a parameter or of its last gradient (FP32) */
+int dpg_mlp_get(const dpg_mlp *mlp, int which, int grad, float *host);
+int dpg_mlp_set(dpg_mlp *mlp, int which, const float *host);
+
+/* per node: normalised state + occupancy patch (80 bf16 per node) from the
+ * context's environment; x_dev N x nx doubles */
+int dpg_mlp_node_features(dpg_ctx *ctx, const double *x_dev, int64_t N, void *feat_dev);
+
+/* scores n pairs: out_dev[n x 2] = [logit, cost-to-go] (FP32) */
+int dpg_mlp_forward(dpg_mlp *mlp, const void *node_feat_dev, const uint32_t *node_dev, const uint32_t *prim_dev,
+                    int64_t n, float *out_dev);
+
+/* one Adam step on a batch: target_dev[B x 2] = [collision (0/1), cost-to-go];
+ * loss = mean(BCE(logit) + 0.5 ctg_weight (ctg - target)^2), returned in *loss */
+int dpg_mlp_train_step(dpg_mlp *mlp, const void *node_feat_dev, const uint32_t *node_dev,
+                       const uint32_t *prim_dev, const float *target_dev, int64_t B, float lr, float ctg_weight,
+                       float *loss);
+
+/* device time of the last forward / train step (ms) and the FLOPs it ran */
+int dpg_mlp_last_timing(const dpg_mlp *mlp, double *ms, double *flops);
+
 #ifdef __cplusplus
 }
 #endif
