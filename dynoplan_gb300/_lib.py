@@ -41,7 +41,7 @@ class RobotDesc(C.Structure):
 class ExpandOpts(C.Structure):
     _fields_ = [
         ("radius", C.c_double), ("precision", C.c_int32), ("x_on_device", C.c_int32),
-        ("out_on_device", C.c_int32), ("reserved", C.c_int32),
+        ("out_on_device", C.c_int32), ("mode", C.c_int32),
         ("contact_band", C.c_double), ("ball_band", C.c_double),
     ]
 
@@ -71,6 +71,8 @@ SIGNATURES = [
                              C.POINTER(ExpandOut)]),
     ("dpg_expand_noalloc", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p,
                                      C.POINTER(ExpandOut)]),
+    ("dpg_check_pairs", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p, C.c_int64,
+                                  C.c_void_p, C.c_void_p, C.POINTER(ExpandOut)]),
     ("dpg_sync", C.c_int, [C.c_void_p]),
     ("dpg_set_abort", C.c_int, [C.c_void_p, C.c_int32]),
     ("dpg_host_alloc", C.c_void_p, [C.c_size_t]),

@@ -360,14 +360,15 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   else if (collided) { verdict = DPG_COLLISION; fi = first_col; }
   else { verdict = DPG_VALID; fi = L; }
   const int er = first_oob < L ? first_oob : L - 1;  // end-state row
-  if (o.verdict) o.verdict[pair] = verdict;
-  if (o.first_invalid) o.first_invalid[pair] = (int16_t)fi;
+  const int64_t row_out = o.out_index ? (int64_t)o.out_index[pair] : pair;
+  if (o.verdict) o.verdict[row_out] = verdict;
+  if (o.first_invalid) o.first_invalid[row_out] = (int16_t)fi;
   if (o.min_gap)
-    o.min_gap[pair] = verdict == DPG_OUT_OF_BOUNDS ? __int_as_float(0x7fc00000)
+    o.min_gap[row_out] = verdict == DPG_OUT_OF_BOUNDS ? __int_as_float(0x7fc00000)
                                                    : ((float)mg <= kGapCap ? (float)mg : __int_as_float(0x7f800000));
-  if (o.flags) o.flags[pair] = rechecked ? DPG_FLAG_CONTACT_RECHECK : 0;
+  if (o.flags) o.flags[row_out] = rechecked ? DPG_FLAG_CONTACT_RECHECK : 0;
   if (o.end_state) {
-    Real *es = (Real *)o.end_state + pair * R::NX;
+    Real *es = (Real *)o.end_state + row_out * R::NX;
     const Real t = Real(er) * dtR;
     const int64_t row = s0 + er;
 #pragma unroll

@@ -55,6 +55,7 @@ struct dpg_ctx {
   // per-call arena
   DevBuf x64, nkey32, noff32, mask, cnt, tot, pbase, ord_pbase, ord_ibase;
   DevBuf p_node, p_prim, p_verdict, p_fi, p_end, p_gap, p_flags;
+  DevBuf q_node, q_prim, q_sorted, q_idx, q_fill;  // dpg_check_pairs
   DevCounters *d_ctr = nullptr;
   DevCounters *h_ctr = nullptr;  // pinned
   int *h_abort = nullptr;        // mapped pinned
@@ -248,7 +249,8 @@ void dpg_destroy(dpg_ctx *c) {
                     &c->st32, &c->act64, &c->pose32, &c->pose64, &c->pbox, &c->pbox32, &c->obs32, &c->obs64,
                     &c->x64, &c->nkey32, &c->noff32, &c->mask, &c->cnt, &c->tot, &c->pbase,
                     &c->ord_pbase, &c->ord_ibase, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
-                    &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32};
+                    &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32,
+                    &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill};
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
@@ -562,7 +564,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
       kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
     };
-    if (fp64) {
+    if (opts->mode & DPG_MODE_BALL_ONLY) {
+      // pairs only: no exact check
+    } else if (fp64) {
       if (cull) launch(check_pairs<KIND, double, false, true>, obs_bytes64);
       else launch(check_pairs<KIND, double, false, false>, obs_bytes64);
     } else {
@@ -590,8 +594,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
         {out->node, c->p_node.p, 4}, {out->prim, c->p_prim.p, 4}, {out->verdict, c->p_verdict.p, 1},
         {out->first_invalid, c->p_fi.p, 2}, {out->end_state, c->p_end.p, es_bytes * nx},
         {out->min_gap, c->p_gap.p, 4}, {out->flags, c->p_flags.p, 1}};
-    for (auto &e : cp)
-      if (e.dst) CUDA_TRY(c, cudaMemcpyAsync(e.dst, e.src, e.b * np, cudaMemcpyDeviceToHost, st));
+    const int n_copy = (opts->mode & DPG_MODE_BALL_ONLY) ? 2 : 7;  // pairs only: node, prim
+    for (int i = 0; i < n_copy; i++)
+      if (cp[i].dst) CUDA_TRY(c, cudaMemcpyAsync(cp[i].dst, cp[i].src, cp[i].b * np, cudaMemcpyDeviceToHost, st));
   } else if (dev_out && np > 0) {
     // node / prim live in the arena unless the caller gave arrays
   }
@@ -840,5 +845,185 @@ extern "C" int dpg_mlp_node_features(dpg_ctx *c, const double *x_dev, int64_t N,
   });
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return DPG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Exact check of an explicit pair list (dpg_check_pairs, dpg.h): the pairs
+// are grouped by primitive (longest first) so the same persistent warps as
+// in dpg_expand walk one primitive per warp; results go back to the input
+// positions.
+extern "C" int dpg_check_pairs(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double *x, int64_t n,
+                               const uint32_t *node, const uint32_t *prim, dpg_expand_out *out) {
+  if (!c || !opts || !out) return DPG_ERR_ARG;
+  if (!c->have_prims || !c->have_env) return fail(c, DPG_ERR_STATE, "check_pairs: upload primitives and env first");
+  if (N < 0 || n < 0 || (N > 0 && !x) || (n > 0 && (!node || !prim)))
+    return fail(c, DPG_ERR_ARG, "check_pairs: bad arrays");
+  if (n > (int64_t)0xffffffffLL || N > (int64_t)1 << 31) return fail(c, DPG_ERR_ARG, "check_pairs: too many pairs");
+  if (out->capacity < n) {
+    out->n_pairs = n;
+    return fail(c, DPG_ERR_CAPACITY, "check_pairs: capacity below n");
+  }
+  if (opts->precision != DPG_FP32 && opts->precision != DPG_FP64) return fail(c, DPG_ERR_ARG, "check_pairs: precision");
+  if (*(volatile int *)c->h_abort) return fail(c, DPG_ERR_ABORTED, "check_pairs: abort flag raised");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  out->n_pairs = n;
+  out->n_scanned = 0;
+  out->n_contact_recheck = 0;
+  out->n_ball_recheck = 0;
+  if (n == 0) return DPG_OK;
+  const int kind = c->robot.kind, nx = c->robot.nx, P = c->P;
+  const int kd = key_dim(kind), od = off_dim(kind);
+  const bool fp64 = opts->precision == DPG_FP64;
+  const size_t es_bytes = fp64 ? sizeof(double) : sizeof(float);
+  const bool dev_in = opts->x_on_device != 0, dev_out = opts->out_on_device != 0;
+  cudaStream_t st = c->stream;
+  int rc;
+  if ((rc = ensure(c, c->x64, sizeof(double) * nx * std::max<int64_t>(N, 1))) ||
+      (rc = ensure(c, c->nkey32, sizeof(float) * kd * std::max<int64_t>(N, 1))) ||
+      (rc = ensure(c, c->noff32, sizeof(float) * od * std::max<int64_t>(N, 1))) ||
+      (rc = ensure(c, c->tot, sizeof(uint32_t) * P)) || (rc = ensure(c, c->q_fill, sizeof(uint32_t) * P)) ||
+      (rc = ensure(c, c->pbase, sizeof(unsigned long long) * P)) ||
+      (rc = ensure(c, c->ord_pbase, sizeof(unsigned long long) * (P + 1))) ||
+      (rc = ensure(c, c->ord_ibase, sizeof(unsigned long long) * (P + 1))) ||
+      (rc = ensure(c, c->q_sorted, 4 * (size_t)n)) || (rc = ensure(c, c->q_idx, 4 * (size_t)n)))
+    return rc;
+  const uint32_t *node_d = node, *prim_d = prim;
+  const double *x_d = x;
+  if (!dev_in) {
+    if ((rc = ensure(c, c->q_node, 4 * (size_t)n)) || (rc = ensure(c, c->q_prim, 4 * (size_t)n))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->x64.p, x, sizeof(double) * nx * std::max<int64_t>(N, 0), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(c, cudaMemcpyAsync(c->q_node.p, node, 4 * n, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(c, cudaMemcpyAsync(c->q_prim.p, prim, 4 * n, cudaMemcpyHostToDevice, st));
+    node_d = P_<uint32_t>(c->q_node);
+    prim_d = P_<uint32_t>(c->q_prim);
+    x_d = P_<double>(c->x64);
+  }
+  PairView po{};
+  po.cap = n;
+  po.node = P_<uint32_t>(c->q_sorted);
+  po.prim = nullptr;
+  po.out_index = P_<uint32_t>(c->q_idx);
+  if (dev_out) {
+    po.verdict = out->verdict;
+    po.first_invalid = out->first_invalid;
+    po.end_state = out->end_state;
+    po.min_gap = out->min_gap;
+    po.flags = out->flags;
+  } else {
+    const size_t nz = (size_t)n;
+    if ((rc = ensure(c, c->p_verdict, nz)) || (rc = ensure(c, c->p_fi, 2 * nz)) ||
+        (rc = ensure(c, c->p_end, es_bytes * nx * nz)) || (rc = ensure(c, c->p_gap, 4 * nz)) ||
+        (rc = ensure(c, c->p_flags, nz)))
+      return rc;
+    po.verdict = out->verdict ? P_<uint8_t>(c->p_verdict) : nullptr;
+    po.first_invalid = out->first_invalid ? P_<int16_t>(c->p_fi) : nullptr;
+    po.end_state = out->end_state ? c->p_end.p : nullptr;
+    po.min_gap = out->min_gap ? P_<float>(c->p_gap) : nullptr;
+    po.flags = out->flags ? P_<uint8_t>(c->p_flags) : nullptr;
+  }
+  PrimView pv{};
+  pv.P = P;
+  pv.S = c->S;
+  pv.len = P_<int32_t>(c->len);
+  pv.soff = P_<int64_t>(c->soff);
+  pv.order = P_<int32_t>(c->order);
+  pv.key32 = P_<float>(c->key32);
+  pv.kconst32 = P_<float>(c->kconst32);
+  pv.st64 = P_<double>(c->st64);
+  pv.st32 = P_<float>(c->st32);
+  pv.pose32 = P_<Pose<float>>(c->pose32);
+  pv.pose64 = P_<Pose<double>>(c->pose64);
+  pv.pbox = P_<double>(c->pbox);
+  pv.pbox32 = P_<float>(c->pbox32);
+  pv.coff = P_<int64_t>(c->coff);
+  pv.cbox32 = P_<float>(c->cbox32);
+  pv.tbox32 = P_<float>(c->tbox32);
+  NodeView nv{N, x_d, P_<float>(c->nkey32), P_<float>(c->noff32)};
+  EnvView ev{};
+  ev.dim = c->dim;
+  for (int i = 0; i < 3; i++) { ev.lo[i] = c->lo[i]; ev.hi[i] = c->hi[i]; }
+  ev.n_obs = c->n_obs;
+  ev.obs32 = c->obs32.p;
+  ev.obs64 = c->obs64.p;
+  const RobotParams rp = c->rp;
+  const double band = opts->contact_band > 0 ? opts->contact_band : 1e-4;
+  CheckArgs ca{};
+  ca.rp = rp;
+  ca.pv = pv;
+  ca.nv = nv;
+  ca.ev = ev;
+  ca.out = po;
+  ca.ord_pbase = P_<unsigned long long>(c->ord_pbase);
+  ca.ord_ibase = P_<unsigned long long>(c->ord_ibase);
+  ca.ctr = c->d_ctr;
+  ca.abort_flag = c->d_abort;
+  ca.band = fp64 ? 0.0 : band;
+  ca.cull_margin = kGapCap + (float)band + 1e-3f;
+  ca.dt32 = (float)rp.dt;
+  ca.half_len32 = (float)rp.half_len;
+  ca.half_wid32 = (float)rp.half_wid;
+  ca.radius32 = (float)rp.radius;
+  ca.band32 = (float)ca.band;
+  for (int i = 0; i < 3; i++) { ca.lo32[i] = (float)c->lo[i]; ca.hi32[i] = (float)c->hi[i]; }
+  const bool cull = c->n_obs <= kMaxCullObs;
+
+  CUDA_TRY(c, cudaEventRecord(c->ev[1], st));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), st));
+  CUDA_TRY(c, cudaMemsetAsync(c->tot.p, 0, sizeof(uint32_t) * P, st));
+  CUDA_TRY(c, cudaMemsetAsync(c->q_fill.p, 0, sizeof(uint32_t) * P, st));
+  cudaError_t launch_err = cudaSuccess;
+  with_kind(kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    using R = Robot<KIND>;
+    if (N > 0) prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
+    pairs_hist<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(prim_d, n, P_<uint32_t>(c->tot));
+    scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), P_<uint32_t>(c->tot), P_<unsigned long long>(c->pbase),
+                                    P_<unsigned long long>(c->ord_pbase), P_<unsigned long long>(c->ord_ibase), n,
+                                    c->d_ctr);
+    pairs_scatter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(node_d, prim_d, n, P_<unsigned long long>(c->pbase),
+                                                               P_<uint32_t>(c->q_fill), P_<uint32_t>(c->q_sorted),
+                                                               P_<uint32_t>(c->q_idx));
+    cudaEventRecord(c->ev[2], st);
+    const size_t obs_bytes = fp64 ? (R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>))
+                                  : (R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>));
+    auto launch = [&](auto kern) {
+      const size_t sm = obs_bytes * std::max(c->n_obs, 1);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
+      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+    };
+    if (fp64) {
+      if (cull) launch(check_pairs<KIND, double, false, true>);
+      else launch(check_pairs<KIND, double, false, false>);
+    } else {
+      if (cull) launch(check_pairs<KIND, float, true, true>);
+      else launch(check_pairs<KIND, float, true, false>);
+    }
+    cudaEventRecord(c->ev[3], st);
+    launch_err = cudaGetLastError();
+  });
+  if (launch_err != cudaSuccess)
+    return fail(c, DPG_ERR_CUDA, std::string("check_pairs launch: ") + cudaGetErrorString(launch_err));
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+  if (!dev_out) {
+    struct { void *dst; void *src; size_t b; } cp[] = {
+        {out->verdict, c->p_verdict.p, 1}, {out->first_invalid, c->p_fi.p, 2},
+        {out->end_state, c->p_end.p, es_bytes * nx}, {out->min_gap, c->p_gap.p, 4}, {out->flags, c->p_flags.p, 1}};
+    for (auto &e : cp)
+      if (e.dst) CUDA_TRY(c, cudaMemcpyAsync(e.dst, e.src, e.b * n, cudaMemcpyDeviceToHost, st));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  const DevCounters h = *c->h_ctr;
+  out->n_contact_recheck = (int64_t)h.n_recheck;
+  if (h.status == DPG_ERR_ABORTED) return fail(c, DPG_ERR_ABORTED, "check_pairs: aborted");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
+  c->timings[0] = ms;
+  cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+  c->timings[1] = ms;
+  c->timings[2] = 0;
+  c->timings[3] = 0;
   return DPG_OK;
 }

@@ -94,6 +94,7 @@ struct PairView {
   void *end_state;     // float or double rows of NX
   float *min_gap;
   uint8_t *flags;
+  const uint32_t *out_index;  // when set, results of pair i go to row out_index[i]
 };
 
 __device__ __forceinline__ float wrap_pi_f64(double a) {
@@ -434,6 +435,29 @@ __global__ void build_chunks(RobotParams rp, int P, const int32_t *len, const in
     tb[i] = c32;
     tb[D + i] = __double2float_ru(half + fabs(cen - (double)c32));
   }
+}
+
+}  // namespace dpg
+
+namespace dpg {
+
+// ---- explicit pair lists (dpg_check_pairs): group pairs by primitive -----
+static __global__ void pairs_hist(const uint32_t *prim, int64_t n, uint32_t *hist) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&hist[prim[i]], 1u);
+}
+
+// position of pair i inside its primitive's segment (order within a segment
+// is arbitrary; results are written back at the input positions)
+static __global__ void pairs_scatter(const uint32_t *node, const uint32_t *prim, int64_t n,
+                                     const unsigned long long *pbase, uint32_t *fill, uint32_t *sorted_node,
+                                     uint32_t *sorted_idx) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t p = prim[i];
+  const unsigned long long pos = pbase[p] + atomicAdd(&fill[p], 1u);
+  sorted_node[pos] = node[i];
+  sorted_idx[pos] = (uint32_t)i;
 }
 
 }  // namespace dpg

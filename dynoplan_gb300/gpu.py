@@ -118,15 +118,39 @@ class Context:
         check(self.lib.dpg_upload_env(self.h, len(lo), _ptr(lo), _ptr(hi), n,
                                       _ptr(olo) if n else None, _ptr(ohi) if n else None), self.h)
 
+    def check_pairs(self, x: np.ndarray, node: np.ndarray, prim: np.ndarray, precision: int = 0,
+                    contact_band: float = 1e-4) -> ExpandResult:
+        """Exact check of the given (node, primitive) pairs; results in input order."""
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, self.nx)
+        node = np.ascontiguousarray(node, dtype=np.uint32)
+        prim = np.ascontiguousarray(prim, dtype=np.uint32)
+        n = len(node)
+        es_dtype = np.float64 if precision == 1 else np.float32
+        o = dict(verdict=np.empty(n, np.uint8), first_invalid=np.empty(n, np.int16),
+                 end_state=np.empty((n, self.nx), es_dtype), min_gap=np.empty(n, np.float32),
+                 flags=np.empty(n, np.uint8))
+        opts = ExpandOpts(radius=0.0, precision=precision, x_on_device=0, out_on_device=0, mode=0,
+                          contact_band=contact_band, ball_band=1e-5)
+        out = ExpandOut(capacity=n)
+        for k, v in o.items():
+            setattr(out, k, _ptr(v))
+        check(self.lib.dpg_check_pairs(self.h, C.byref(opts), len(x), _ptr(x), n, _ptr(node), _ptr(prim),
+                                       C.byref(out)), self.h)
+        res = ExpandResult(o)
+        res.update(node=node, prim=prim, n_pairs=n, n_contact_recheck=int(out.n_contact_recheck))
+        return res
+
     def expand(self, x: np.ndarray, radius: float, precision: int = 0, capacity: int | None = None,
-               contact_band: float = 1e-4, ball_band: float = 1e-5, outputs=None) -> ExpandResult:
-        """Batched expand of the rows of x (N x nx), results in host arrays."""
+               contact_band: float = 1e-4, ball_band: float = 1e-5, outputs=None,
+               ball_only: bool = False) -> ExpandResult:
+        """Batched expand of the rows of x (N x nx), results in host arrays.
+        ball_only: the in-ball (node, prim) pairs without the exact check."""
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, self.nx)
         N = len(x)
         if capacity is None:
             capacity = max(1024, N * 64)
         opts = ExpandOpts(radius=radius, precision=precision, x_on_device=0, out_on_device=0,
-                          reserved=0, contact_band=contact_band, ball_band=ball_band)
+                          mode=1 if ball_only else 0, contact_band=contact_band, ball_band=ball_band)
         while True:
             es_dtype = np.float64 if precision == 1 else np.float32
             o = outputs if outputs is not None else dict(
@@ -156,7 +180,7 @@ class Context:
         """Expand with the nodes and all outputs in device memory (raw device
         pointers); returns the counters."""
         opts = ExpandOpts(radius=radius, precision=precision, x_on_device=1, out_on_device=1,
-                          reserved=0, contact_band=contact_band, ball_band=ball_band)
+                          mode=0, contact_band=contact_band, ball_band=ball_band)
         out = ExpandOut(capacity=capacity)
         for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap", "flags"):
             setattr(out, k, C.c_void_p(out_ptrs[k]) if out_ptrs.get(k) else None)

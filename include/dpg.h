@@ -67,6 +67,9 @@ extern "C" {
 #define DPG_FP32 0
 #define DPG_FP64 1
 
+/* dpg_expand_opts.mode */
+#define DPG_MODE_BALL_ONLY 1
+
 /* per-pair flags */
 #define DPG_FLAG_CONTACT_RECHECK 1 /* verdict recomputed in FP64 (contact/bounds band) */
 
@@ -96,7 +99,8 @@ typedef struct dpg_expand_opts {
   int32_t precision;      /* DPG_FP32 or DPG_FP64 */
   int32_t x_on_device;    /* x is a device pointer */
   int32_t out_on_device;  /* output arrays are device pointers */
-  int32_t reserved;
+  int32_t mode;           /* 0: full expand; DPG_MODE_BALL_ONLY: in-ball pairs only
+                             (node, prim), no exact check */
   double contact_band;    /* FP64 re-check band for gaps and bounds (1e-4) */
   double ball_band;       /* FP64 re-check band around the radius (1e-5) */
 } dpg_expand_opts;
@@ -153,6 +157,16 @@ int dpg_upload_env(dpg_ctx *ctx, int32_t dim, const double *lo, const double *hi
  * out->n_pairs set when out->capacity is too small. */
 int dpg_expand(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x,
                dpg_expand_out *out);
+
+/* Exact check of an explicit list of n (node, primitive) pairs -- the lazy
+ * check_lazy_trajectory of src/dbastar/dbastar.cpp:391-490 for a batch of
+ * candidates chosen by the caller (e.g. ordered by the surrogate, or the
+ * pairs a search still needs).  node[i] indexes the N states in x, prim[i]
+ * the uploaded primitives.  Outputs are written at the input positions i;
+ * opts->radius is ignored; opts->x_on_device applies to x, node and prim;
+ * out->capacity must be >= n (out->node / out->prim are not written). */
+int dpg_check_pairs(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x, int64_t n,
+                    const uint32_t *node, const uint32_t *prim, dpg_expand_out *out);
 
 /* Allocation-free form of dpg_expand.  No counterpart in the reference (its
  * expansion runs on the host).  For callers that cannot allocate device

@@ -36,7 +36,7 @@ def _device_out(torch, cap, nx, precision):
 
 def _call(lib, ctx, x_d, N, outs, cap, radius, precision):
     from dynoplan_gb300._lib import ExpandOpts, ExpandOut
-    opts = ExpandOpts(radius=radius, precision=precision, x_on_device=1, out_on_device=1, reserved=0,
+    opts = ExpandOpts(radius=radius, precision=precision, x_on_device=1, out_on_device=1, mode=0,
                       contact_band=1e-4, ball_band=1e-5)
     out = ExpandOut(capacity=cap)
     for k, t in outs.items():
