@@ -91,6 +91,9 @@ SIGNATURES = [
     ("dpg_mlp_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                      C.c_float, C.c_float, C.POINTER(C.c_float)]),
     ("dpg_mlp_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    # include/dpg_search.h
+    ("dpg_search", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                             C.c_void_p, C.c_void_p, C.c_int32]),
     # include/dpg_bench.h
     ("dpg_bench_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("dpg_bench_flush_l2", C.c_int, [C.c_int, C.c_size_t]),

@@ -1,0 +1,56 @@
+// ctx.h -- the context behind the opaque dpg_ctx handle of include/dpg.h
+// (shared by the translation units of the library; not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "dpg.h"
+#include "expand_kernels.cuh"
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct dpg_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  dpg_robot_desc robot{};
+  dpg::RobotParams rp{};
+  std::string err;
+
+  // primitives
+  bool have_prims = false;
+  int P = 0;
+  int64_t S = 0, A = 0;
+  std::vector<int32_t> h_len, h_order;
+  std::vector<int64_t> h_soff, h_aoff, h_coff;
+  DevBuf len, soff, aoff, order, key32, kconst32, st64, st32, act64, pose32, pose64, pbox, pbox32;
+  DevBuf coff, cbox32, tbox32;
+
+  // environment
+  bool have_env = false;
+  int dim = 0;
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  int n_obs = 0;
+  DevBuf obs32, obs64;
+
+  // per-call arena
+  DevBuf x64, nkey32, noff32, mask, cnt, tot, pbase, ord_pbase, ord_ibase;
+  DevBuf p_node, p_prim, p_verdict, p_fi, p_end, p_gap, p_flags;
+  DevBuf q_node, q_prim, q_sorted, q_idx, q_fill;  // dpg_check_pairs
+  dpg::DevCounters *d_ctr = nullptr;
+  dpg::DevCounters *h_ctr = nullptr;  // pinned
+  int *h_abort = nullptr;             // mapped pinned
+  int *d_abort = nullptr;
+  cudaEvent_t ev[6] = {};
+  double timings[4] = {0, 0, 0, 0};
+};
+
+// canonical FP64 state rows of the uploaded primitives ([S][nx], the device
+// table after the canonical rollout), copied to the host on first use
+int dpg_ctx_host_states(dpg_ctx *c, std::vector<double> &out);

@@ -1,0 +1,521 @@
+// search.cu -- db-A* over the batched GPU expansion (include/dpg_search.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <queue>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+#include "dpg_mlp.h"
+#include "dpg_search.h"
+#include "mlp_kernels.cuh"
+
+using namespace dpg;
+
+namespace {
+
+constexpr double kTwoPiH = 6.283185307179586476925286766559;
+constexpr double kPiH = 3.1415926535897932384626433832795;
+
+double so2(double a, double b) {
+  double d = std::fabs(a - b);
+  d = std::fmod(d, kTwoPiH);
+  return d > kPiH ? kTwoPiH - d : d;
+}
+double n3(double a, double b, double c) { return std::sqrt(a * a + b * b + c * c); }
+
+// robot metric and time lower bound: the definitions the checker's tables use
+// (weighted sum of block distances; lower_bound_time = max over blocks of
+// distance / max speed)
+double distance(const dpg_robot_desc &r, const double *a, const double *b) {
+  const double *w = r.w;
+  switch (r.kind) {
+    case DPG_ROBOT_UNICYCLE1: return w[0] * std::hypot(a[0] - b[0], a[1] - b[1]) + w[1] * so2(a[2], b[2]);
+    case DPG_ROBOT_CAR1:
+      return w[0] * std::hypot(a[0] - b[0], a[1] - b[1]) + w[1] * so2(a[2], b[2]) + w[2] * so2(a[3], b[3]);
+    case DPG_ROBOT_QUAD2D:
+      return w[0] * std::hypot(a[0] - b[0], a[1] - b[1]) + w[1] * so2(a[2], b[2]) +
+             w[2] * std::hypot(a[3] - b[3], a[4] - b[4]) + w[3] * std::fabs(a[5] - b[5]);
+    default: {
+      double dq = std::fabs(a[3] * b[3] + a[4] * b[4] + a[5] * b[5] + a[6] * b[6]);
+      dq = std::min(dq, 1.0);
+      return w[0] * n3(a[0] - b[0], a[1] - b[1], a[2] - b[2]) + w[1] * std::acos(dq) +
+             w[2] * n3(a[7] - b[7], a[8] - b[8], a[9] - b[9]) + w[3] * n3(a[10] - b[10], a[11] - b[11], a[12] - b[12]);
+    }
+  }
+}
+
+double lower_bound_time(const dpg_robot_desc &r, const double *a, const double *b) {
+  switch (r.kind) {
+    case DPG_ROBOT_UNICYCLE1:
+      return std::max(std::hypot(a[0] - b[0], a[1] - b[1]) / 0.5, so2(a[2], b[2]) / 0.5);
+    case DPG_ROBOT_CAR1:
+      return std::max(std::max(std::hypot(a[0] - b[0], a[1] - b[1]) / 0.5, so2(a[2], b[2]) / 0.5), so2(a[3], b[3]) / 0.5);
+    case DPG_ROBOT_QUAD2D:
+      return std::max(std::max(std::hypot(a[0] - b[0], a[1] - b[1]) / 2.0, so2(a[2], b[2]) / 4.0),
+                      std::max(std::hypot(a[3] - b[3], a[4] - b[4]) / 4.0, std::fabs(a[5] - b[5]) / 8.0));
+    default: {
+      double dq = std::fabs(a[3] * b[3] + a[4] * b[4] + a[5] * b[5] + a[6] * b[6]);
+      dq = std::min(dq, 1.0);
+      return std::max(std::max(n3(a[0] - b[0], a[1] - b[1], a[2] - b[2]) / 4.0, std::acos(dq) / 8.0),
+                      std::max(n3(a[7] - b[7], a[8] - b[8], a[9] - b[9]) / 4.0,
+                               n3(a[10] - b[10], a[11] - b[11], a[12] - b[12]) / 8.0));
+    }
+  }
+}
+
+// components shifted by the node offset: positions, then velocities
+int offset_comps(int kind, int *pos, int *vel) {
+  switch (kind) {
+    case DPG_ROBOT_QUAD2D: pos[0] = 0; pos[1] = 1; vel[0] = 3; vel[1] = 4; return 2;
+    case DPG_ROBOT_QUAD3D:
+      pos[0] = 0; pos[1] = 1; pos[2] = 2; vel[0] = 7; vel[1] = 8; vel[2] = 9; return 3;
+    default: pos[0] = 0; pos[1] = 1; return 2;
+  }
+}
+bool has_vel(int kind) { return kind == DPG_ROBOT_QUAD2D || kind == DPG_ROBOT_QUAD3D; }
+
+// state k of primitive p applied at node x (FP64, the transform of the tables)
+void transformed_state(const dpg_robot_desc &r, const std::vector<double> &st, int64_t row0, int k,
+                       const double *x, double *out) {
+  const int nx = r.nx;
+  std::memcpy(out, st.data() + (row0 + k) * nx, sizeof(double) * nx);
+  int pos[3], vel[3];
+  const int d = offset_comps(r.kind, pos, vel);
+  const bool v = has_vel(r.kind);
+  const double t = k * r.dt;
+  for (int i = 0; i < d; i++) {
+    out[pos[i]] += x[pos[i]];
+    if (v) {
+      out[pos[i]] += t * x[vel[i]];
+      out[vel[i]] += x[vel[i]];
+    }
+  }
+}
+
+// ---- GPU radius query: for each query q, the targets within radius ------
+// (full-state metric, FP32 with an FP64 re-test within `band` of the radius)
+template <int KIND>
+__device__ float full_dist32(const float4 w, const float *a, const float *b) {
+  auto so2f = [](float x, float y) {
+    float d = fabsf(x - y);
+    d = fmodf(d, 6.2831853071795865f);
+    return d > 3.1415926535897932f ? 6.2831853071795865f - d : d;
+  };
+  if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
+    return w.x * hypotf(a[0] - b[0], a[1] - b[1]) + w.y * so2f(a[2], b[2]);
+  } else if constexpr (KIND == DPG_ROBOT_CAR1) {
+    return w.x * hypotf(a[0] - b[0], a[1] - b[1]) + w.y * so2f(a[2], b[2]) + w.z * so2f(a[3], b[3]);
+  } else if constexpr (KIND == DPG_ROBOT_QUAD2D) {
+    return w.x * hypotf(a[0] - b[0], a[1] - b[1]) + w.y * so2f(a[2], b[2]) + w.z * hypotf(a[3] - b[3], a[4] - b[4]) +
+           w.w * fabsf(a[5] - b[5]);
+  } else {
+    float dq = fminf(1.f, fabsf(a[3] * b[3] + a[4] * b[4] + a[5] * b[5] + a[6] * b[6]));
+    auto l3 = [](float x, float y, float z) { return sqrtf(x * x + y * y + z * z); };
+    return w.x * l3(a[0] - b[0], a[1] - b[1], a[2] - b[2]) + w.y * acosf(dq) +
+           w.z * l3(a[7] - b[7], a[8] - b[8], a[9] - b[9]) + w.w * l3(a[10] - b[10], a[11] - b[11], a[12] - b[12]);
+  }
+}
+
+template <int KIND>
+__device__ double full_dist64(const RobotParams &rp, const double *a, const double *b) {
+  auto so2d = [](double x, double y) {
+    double d = fabs(x - y);
+    d = fmod(d, kTwoPi);
+    return d > kPi ? kTwoPi - d : d;
+  };
+  if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
+    return rp.w[0] * hypot(a[0] - b[0], a[1] - b[1]) + rp.w[1] * so2d(a[2], b[2]);
+  } else if constexpr (KIND == DPG_ROBOT_CAR1) {
+    return rp.w[0] * hypot(a[0] - b[0], a[1] - b[1]) + rp.w[1] * so2d(a[2], b[2]) + rp.w[2] * so2d(a[3], b[3]);
+  } else if constexpr (KIND == DPG_ROBOT_QUAD2D) {
+    return rp.w[0] * hypot(a[0] - b[0], a[1] - b[1]) + rp.w[1] * so2d(a[2], b[2]) +
+           rp.w[2] * hypot(a[3] - b[3], a[4] - b[4]) + rp.w[3] * fabs(a[5] - b[5]);
+  } else {
+    double dq = fmin(1.0, fabs(a[3] * b[3] + a[4] * b[4] + a[5] * b[5] + a[6] * b[6]));
+    auto l3 = [](double x, double y, double z) { return sqrt(x * x + y * y + z * z); };
+    return rp.w[0] * l3(a[0] - b[0], a[1] - b[1], a[2] - b[2]) + rp.w[1] * acos(dq) +
+           rp.w[2] * l3(a[7] - b[7], a[8] - b[8], a[9] - b[9]) + rp.w[3] * l3(a[10] - b[10], a[11] - b[11], a[12] - b[12]);
+  }
+}
+
+// block y = query; threads stride over targets.  Targets are rows of nx
+// doubles (FP64) mirrored as FP32.  lower_only: only targets t < q (a query
+// set against itself).  Up to K ids per query (count may exceed K).
+template <int KIND>
+__global__ void radius_query(RobotParams rp, float4 w32, const double *q64, const float *q32, int Q, int q_off,
+                             const double *t64, const float *t32, int T, double radius, float band, int lower_only,
+                             int K, int *count, int *ids) {
+  using R = Robot<KIND>;
+  const int q = blockIdx.y + q_off;
+  if (q >= Q) return;
+  float a[R::NX];
+#pragma unroll
+  for (int i = 0; i < R::NX; i++) a[i] = q32[(int64_t)q * R::NX + i];
+  const int tend = lower_only ? min(T, q) : T;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tend; t += gridDim.x * blockDim.x) {
+    float b[R::NX];
+#pragma unroll
+    for (int i = 0; i < R::NX; i++) b[i] = t32[(int64_t)t * R::NX + i];
+    const float d = full_dist32<KIND>(w32, a, b);
+    bool in = d <= (float)radius;
+    if (fabsf(d - (float)radius) <= band)
+      in = full_dist64<KIND>(rp, q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX) <= radius;
+    if (in) {
+      const int slot = atomicAdd(&count[q], 1);
+      if (slot < K) ids[(int64_t)q * K + slot] = t;
+    }
+  }
+}
+
+template <class F> void with_kind_s(int kind, F &&f) {
+  switch (kind) {
+    case DPG_ROBOT_UNICYCLE1: f(std::integral_constant<int, DPG_ROBOT_UNICYCLE1>{}); break;
+    case DPG_ROBOT_CAR1: f(std::integral_constant<int, DPG_ROBOT_CAR1>{}); break;
+    case DPG_ROBOT_QUAD3D: f(std::integral_constant<int, DPG_ROBOT_QUAD3D>{}); break;
+    case DPG_ROBOT_QUAD2D: f(std::integral_constant<int, DPG_ROBOT_QUAD2D>{}); break;
+  }
+}
+
+struct Node {
+  float g = 0, h = 0, f = 0;  // float scores, as AStarNode (dbastar.hpp:62-64)
+  int parent = -1;
+  int motion = -1;
+  int inter = -1;             // intermediate state index when a goal was met inside the motion
+  int version = 0;
+  bool in_open = false;
+};
+
+struct HeapItem {
+  float f, g;
+  int id, version;
+};
+struct HeapCmp {  // lowest f first, then highest g (compareAStarNode)
+  bool operator()(const HeapItem &a, const HeapItem &b) const {
+    if (a.f != b.f) return a.f > b.f;
+    return a.g < b.g;
+  }
+};
+
+template <class T> struct DVec {  // growable device array
+  T *p = nullptr;
+  size_t cap = 0;
+  ~DVec() { if (p) cudaFree(p); }
+  bool reserve(size_t n) {
+    if (n <= cap) return true;
+    size_t nc = std::max<size_t>(n, cap * 2 + 1024);
+    T *q = nullptr;
+    if (cudaMalloc(&q, sizeof(T) * nc) != cudaSuccess) return false;
+    if (p) {
+      cudaMemcpy(q, p, sizeof(T) * cap, cudaMemcpyDeviceToDevice);
+      cudaFree(p);
+    }
+    p = q;
+    cap = nc;
+    return true;
+  }
+};
+
+struct Cand {
+  int batch_node;   // index into the batch
+  int prim;
+  int chosen;       // intermediate state index (check_goal) or -1
+  double cost;      // motion duration
+  std::vector<double> x;  // successor state
+  std::vector<double> x0; // transformed start of the motion
+};
+
+}  // namespace
+
+int dpg_ctx_host_states(dpg_ctx *c, std::vector<double> &out) {
+  out.resize((size_t)c->S * c->robot.nx);
+  cudaSetDevice(c->device);
+  return cudaMemcpy(out.data(), c->st64.p, sizeof(double) * out.size(), cudaMemcpyDeviceToHost) == cudaSuccess
+             ? DPG_OK
+             : DPG_ERR_CUDA;
+}
+
+extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *start, const double *goal,
+                          dpg_mlp *mlp, dpg_search_result *res, int32_t *path_motion, double *path_state,
+                          int32_t max_path) {
+  if (!c || !o || !start || !goal || !res) return DPG_ERR_ARG;
+  if (!c->have_prims || !c->have_env) return DPG_ERR_STATE;
+  if (!(o->delta > 0) || !(o->alpha > 0 && o->alpha < 1) || o->batch < 1 || o->limit_branching_factor < 1)
+    return DPG_ERR_ARG;
+  if (o->heuristic == DPG_HEU_MLP && !mlp) return DPG_ERR_ARG;
+  std::memset(res, 0, sizeof(*res));
+  const auto t_start = std::chrono::steady_clock::now();
+  auto elapsed_ms = [&] {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  };
+  const dpg_robot_desc &r = c->robot;
+  const int nx = r.nx, P = c->P;
+  std::vector<double> st;
+  int rc = dpg_ctx_host_states(c, st);
+  if (rc) return rc;
+  const double goal_tol = o->delta_factor_goal * o->delta;
+  const double nov_radius = (1.0 - o->alpha) * o->delta;
+  const int K = std::max(1, o->max_neighbors);
+  std::mt19937 rng((uint32_t)o->seed);
+
+  // explored nodes (host) + their states mirrored on the GPU for the queries
+  std::vector<Node> nodes;
+  std::vector<double> xs;  // [nodes][nx]
+  DVec<double> t64;
+  DVec<float> t32;
+  auto add_node = [&](const double *x) {
+    nodes.emplace_back();
+    xs.insert(xs.end(), x, x + nx);
+    return (int)nodes.size() - 1;
+  };
+  size_t uploaded = 0;
+  auto sync_table = [&]() -> bool {
+    const size_t n = nodes.size();
+    if (!t64.reserve(n * nx) || !t32.reserve(n * nx)) return false;
+    if (n > uploaded) {
+      std::vector<float> f(xs.begin() + uploaded * nx, xs.end());
+      cudaMemcpy(t64.p + uploaded * nx, xs.data() + uploaded * nx, sizeof(double) * (n - uploaded) * nx,
+                 cudaMemcpyHostToDevice);
+      cudaMemcpy(t32.p + uploaded * nx, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice);
+      uploaded = n;
+    }
+    return true;
+  };
+  auto heuristic = [&](const double *x) -> float {
+    if (o->heuristic == DPG_HEU_BLIND) return 0.f;
+    return (float)lower_bound_time(r, x, goal);
+  };
+
+  std::priority_queue<HeapItem, std::vector<HeapItem>, HeapCmp> open;
+  const int s0 = add_node(start);
+  nodes[s0].g = 0;
+  nodes[s0].h = heuristic(start);
+  nodes[s0].f = nodes[s0].g + nodes[s0].h;
+  nodes[s0].in_open = true;
+  open.push({nodes[s0].f, nodes[s0].g, s0, 0});
+
+  // per-iteration device buffers
+  DVec<double> q64, b64;
+  DVec<float> q32;
+  DVec<int> cnt_tab, ids_tab, cnt_self, ids_self;
+  DVec<uint32_t> pnode, pprim;
+  DVec<float> mlp_out;
+  DVec<__nv_bfloat16> feat;
+  std::vector<uint32_t> h_node, h_prim;
+  std::vector<uint8_t> h_verdict;
+  std::vector<int16_t> h_fi;
+  int solution = -1;
+  int status = DPG_SEARCH_EMPTY_QUEUE;
+  const float4 w32 = make_float4((float)r.w[0], (float)r.w[1], (float)r.w[2], (float)r.w[3]);
+
+  while (true) {
+    if (res->expands >= o->max_expands) { status = DPG_SEARCH_MAX_EXPANDS; break; }
+    if (elapsed_ms() > o->time_limit_ms) { status = DPG_SEARCH_MAX_TIME; break; }
+    if (open.empty()) { status = DPG_SEARCH_EMPTY_QUEUE; break; }
+    // pop up to `batch` nodes
+    std::vector<int> batch;
+    while (!open.empty() && (int)batch.size() < o->batch &&
+           res->expands + (int64_t)batch.size() < o->max_expands) {
+      const HeapItem it = open.top();
+      open.pop();
+      Node &n = nodes[it.id];
+      if (!n.in_open || it.version != n.version) continue;  // stale entry
+      n.in_open = false;
+      batch.push_back(it.id);
+    }
+    if (batch.empty()) continue;
+    bool solved = false;
+    for (int id : batch) {
+      res->expands++;
+      if (distance(r, &xs[(size_t)id * nx], goal) < goal_tol) {  // dbastar.cpp:790-800
+        solution = id;
+        solved = true;
+        break;
+      }
+    }
+    if (solved) { status = DPG_SEARCH_SOLVED; break; }
+
+    // expand the batch: every in-ball pair, exact-checked
+    const int B = (int)batch.size();
+    std::vector<double> bx((size_t)B * nx);
+    for (int i = 0; i < B; i++) std::memcpy(&bx[(size_t)i * nx], &xs[(size_t)batch[i] * nx], sizeof(double) * nx);
+    int64_t cap = std::max<int64_t>(1024, (int64_t)B * 256);
+    dpg_expand_out eo{};
+    dpg_expand_opts eopt{};
+    eopt.radius = o->alpha * o->delta;
+    eopt.precision = o->precision;
+    eopt.contact_band = 1e-4;
+    eopt.ball_band = 1e-5;
+    const double te0 = elapsed_ms();
+    for (;;) {
+      h_node.resize(cap); h_prim.resize(cap); h_verdict.resize(cap); h_fi.resize(cap);
+      eo = dpg_expand_out{};
+      eo.capacity = cap;
+      eo.node = h_node.data(); eo.prim = h_prim.data(); eo.verdict = h_verdict.data(); eo.first_invalid = h_fi.data();
+      rc = dpg_expand(c, &eopt, B, bx.data(), &eo);
+      if (rc == DPG_ERR_CAPACITY) { cap = eo.n_pairs; continue; }
+      break;
+    }
+    if (rc) return rc;
+    res->expand_ms += elapsed_ms() - te0;
+    res->checked_pairs += eo.n_pairs;
+
+    // candidates per batch node, valid pairs, in expand_lazy's order
+    std::vector<std::vector<int>> per_node(B);
+    for (int64_t i = 0; i < eo.n_pairs; i++)
+      if (h_verdict[i] == DPG_VALID) per_node[h_node[i]].push_back((int)h_prim[i]);
+    std::vector<Cand> cands;
+    std::vector<int> first_cand(B + 1, 0);
+    for (int b = 0; b < B; b++) {
+      auto &v = per_node[b];
+      std::sort(v.begin(), v.end());
+      if (o->shuffle) std::shuffle(v.begin(), v.end(), rng);
+      first_cand[b] = (int)cands.size();
+      const double *x = &bx[(size_t)b * nx];
+      for (int p : v) {
+        Cand cd;
+        cd.batch_node = b;
+        cd.prim = p;
+        const int L = c->h_len[p];
+        cd.x.resize(nx);
+        cd.x0.resize(nx);
+        transformed_state(r, st, c->h_soff[p], L - 1, x, cd.x.data());
+        transformed_state(r, st, c->h_soff[p], 0, x, cd.x0.data());
+        cd.chosen = -1;
+        // check_goal: states at floor((k+1)/(n+1) * L), k = 0..3 (dbastar.cpp:492-512)
+        std::vector<double> xi(nx);
+        for (int k = 0; k < 4; k++) {
+          const int idx = (int)((float)(k + 1) / 5.0f * (float)L);
+          if (idx >= L) continue;
+          transformed_state(r, st, c->h_soff[p], idx, x, xi.data());
+          if (distance(r, xi.data(), goal) <= goal_tol) {
+            cd.x = xi;
+            cd.chosen = idx;
+            break;
+          }
+        }
+        cd.cost = (cd.chosen != -1 ? cd.chosen : L - 1) * r.dt;
+        cands.push_back(std::move(cd));
+      }
+    }
+    first_cand[B] = (int)cands.size();
+    const int Q = (int)cands.size();
+    if (Q == 0) continue;
+
+    // novelty: candidates vs explored nodes, and vs earlier candidates
+    const double tn0 = elapsed_ms();
+    if (!sync_table() || !q64.reserve((size_t)Q * nx) || !q32.reserve((size_t)Q * nx) ||
+        !cnt_tab.reserve(Q) || !ids_tab.reserve((size_t)Q * K) || !cnt_self.reserve(Q) ||
+        !ids_self.reserve((size_t)Q * K))
+      return DPG_ERR_OOM;
+    std::vector<double> qh((size_t)Q * nx);
+    for (int i = 0; i < Q; i++) std::memcpy(&qh[(size_t)i * nx], cands[i].x.data(), sizeof(double) * nx);
+    std::vector<float> qf(qh.begin(), qh.end());
+    cudaMemcpy(q64.p, qh.data(), sizeof(double) * qh.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(q32.p, qf.data(), sizeof(float) * qf.size(), cudaMemcpyHostToDevice);
+    cudaMemset(cnt_tab.p, 0, sizeof(int) * Q);
+    cudaMemset(cnt_self.p, 0, sizeof(int) * Q);
+    const int T = (int)nodes.size();
+    with_kind_s(r.kind, [&](auto Kd) {
+      constexpr int KIND = decltype(Kd)::value;
+      for (int q0 = 0; q0 < Q; q0 += 65535) {  // grid.y limit
+        const int nq = std::min(65535, Q - q0);
+        dim3 g1((unsigned)std::min(64, (T + 255) / 256), (unsigned)nq);
+        radius_query<KIND><<<g1, 256>>>(c->rp, w32, q64.p, q32.p, Q, q0, t64.p, t32.p, T, nov_radius, 1e-5f, 0, K,
+                                        cnt_tab.p, ids_tab.p);
+        dim3 g2((unsigned)std::min(64, (Q + 255) / 256), (unsigned)nq);
+        radius_query<KIND><<<g2, 256>>>(c->rp, w32, q64.p, q32.p, Q, q0, q64.p, q32.p, Q, nov_radius, 1e-5f, 1, K,
+                                        cnt_self.p, ids_self.p);
+      }
+    });
+    std::vector<int> ct(Q), it((size_t)Q * K), cs(Q), is((size_t)Q * K);
+    cudaMemcpy(ct.data(), cnt_tab.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
+    cudaMemcpy(it.data(), ids_tab.p, sizeof(int) * Q * K, cudaMemcpyDeviceToHost);
+    cudaMemcpy(cs.data(), cnt_self.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
+    if (cudaMemcpy(is.data(), ids_self.p, sizeof(int) * Q * K, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return DPG_ERR_CUDA;
+    res->novelty_ms += elapsed_ms() - tn0;
+
+    // insert or rewire, in pop order and the candidates' order (dbastar.cpp:809-919)
+    std::vector<int> accepted_as(Q, -1);  // node id of an accepted candidate
+    for (int b = 0; b < B; b++) {
+      const int parent = batch[b];
+      int n_new = 0;
+      for (int ci = first_cand[b]; ci < first_cand[b + 1]; ci++) {
+        Cand &cd = cands[ci];
+        const double h = (o->heuristic == DPG_HEU_BLIND) ? 0.0 : lower_bound_time(r, cd.x.data(), goal);
+        const double g = (double)nodes[parent].g + cd.cost +
+                         o->cost_delta_factor * lower_bound_time(r, &xs[(size_t)parent * nx], cd.x0.data());
+        std::vector<int> nbr;
+        for (int k = 0; k < std::min(ct[ci], K); k++) nbr.push_back(it[(size_t)ci * K + k]);
+        for (int k = 0; k < std::min(cs[ci], K); k++) {
+          const int other = is[(size_t)ci * K + k];
+          if (accepted_as[other] >= 0) nbr.push_back(accepted_as[other]);
+        }
+        std::sort(nbr.begin(), nbr.end());
+        if (nbr.empty() || cd.chosen != -1) {
+          const int id = add_node(cd.x.data());
+          Node &n = nodes[id];
+          n.g = (float)g;
+          n.h = (float)h;
+          n.f = n.g + n.h;
+          n.parent = parent;
+          n.motion = cd.prim;
+          n.inter = cd.chosen;
+          n.in_open = true;
+          open.push({n.f, n.g, id, n.version});
+          accepted_as[ci] = id;
+          n_new++;
+        } else {
+          for (int nb : nbr) {
+            Node &n = nodes[nb];
+            const double tentative = g + lower_bound_time(r, cd.x.data(), &xs[(size_t)nb * nx]);
+            if (tentative < n.g) {
+              n.g = (float)tentative;
+              n.f = n.g + n.h;
+              n.parent = parent;
+              n.motion = cd.prim;
+              n.inter = -1;
+              n.version++;
+              n.in_open = true;
+              open.push({n.f, n.g, nb, n.version});
+            }
+          }
+        }
+        if (n_new >= o->limit_branching_factor) break;
+      }
+    }
+  }
+  res->status = status;
+  res->nodes = (int64_t)nodes.size();
+  res->time_ms = elapsed_ms();
+  if (solution >= 0) {
+    res->solved = 1;
+    res->g = nodes[solution].g;
+    std::vector<int> chain;
+    for (int id = solution; id != -1; id = nodes[id].parent) chain.push_back(id);
+    std::reverse(chain.begin(), chain.end());
+    res->path_len = (int32_t)chain.size() - 1;
+    double cost = 0;
+    for (size_t i = 1; i < chain.size(); i++) {
+      const Node &n = nodes[chain[i]];
+      const int L = c->h_len[n.motion];
+      cost += (n.inter != -1 ? n.inter : L - 1) * r.dt;
+    }
+    res->cost = cost;
+    for (int i = 0; i < res->path_len && i < max_path; i++) {
+      if (path_motion) path_motion[i] = nodes[chain[i + 1]].motion;
+    }
+    if (path_state)
+      for (int i = 0; i <= res->path_len && i <= max_path; i++)
+        std::memcpy(path_state + (size_t)i * nx, &xs[(size_t)chain[i] * nx], sizeof(double) * nx);
+  }
+  (void)mlp;
+  (void)P;
+  return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
