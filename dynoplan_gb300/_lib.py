@@ -86,7 +86,7 @@ SIGNATURES = [
     ("dpg_mlp_param_size", C.c_int64, [C.c_void_p, C.c_int]),
     ("dpg_mlp_get", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("dpg_mlp_set", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
-    ("dpg_mlp_node_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("dpg_mlp_node_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("dpg_mlp_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("dpg_mlp_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                      C.c_float, C.c_float, C.POINTER(C.c_float)]),

@@ -783,7 +783,8 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
 // ---------------------------------------------------------------------------
 // Node features of the surrogate MLP (include/dpg_mlp.h): normalised state
 // and the occupancy patch of the context's environment around each node.
-extern "C" int dpg_mlp_node_features(dpg_ctx *c, const double *x_dev, int64_t N, void *feat_dev) {
+extern "C" int dpg_mlp_node_features(dpg_ctx *c, const double *x_dev, int64_t N, const double *goal,
+                                     void *feat_dev) {
   if (!c || N < 0 || (N > 0 && (!x_dev || !feat_dev))) return DPG_ERR_ARG;
   if (!c->have_env) return fail(c, DPG_ERR_STATE, "node_features: upload the environment first");
   if (N == 0) return DPG_OK;
@@ -795,10 +796,13 @@ extern "C" int dpg_mlp_node_features(dpg_ctx *c, const double *x_dev, int64_t N,
   ev.n_obs = c->n_obs;
   ev.obs32 = c->obs32.p;
   ev.obs64 = c->obs64.p;
+  GoalView gv{};
+  gv.has = goal ? 1 : 0;
+  for (int i = 0; i < 3 && goal; i++) gv.g[i] = i < c->dim ? goal[i] : 0.0;
   with_kind(c->robot.kind, [&](auto K) {
     constexpr int KIND = decltype(K)::value;
     mlp_node_features<KIND><<<(unsigned)((N + 127) / 128), 128, 0, c->stream>>>(
-        nv, ev, static_cast<__nv_bfloat16 *>(feat_dev));
+        nv, ev, gv, static_cast<__nv_bfloat16 *>(feat_dev));
   });
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));

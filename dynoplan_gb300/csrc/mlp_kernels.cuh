@@ -23,9 +23,16 @@ constexpr int kMlpIn = 128, kMlpNodeFeat = 80, kMlpEmb = 16, kMlpHidden = 256, k
 constexpr int kOccSide = 8;
 constexpr float kOccCell = 0.75f;
 
+// goal the cost-to-go refers to: slots 13.. of the state block hold
+// (goal - position), normalised like the position
+struct GoalView {
+  int has;
+  double g[3];
+};
+
 // per node: normalised state + occupancy patch (80 bf16)
 template <int KIND>
-__global__ void mlp_node_features(NodeView nv, EnvView ev, __nv_bfloat16 *feat) {
+__global__ void mlp_node_features(NodeView nv, EnvView ev, GoalView gv, __nv_bfloat16 *feat) {
   using R = Robot<KIND>;
   const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (n >= nv.N) return;
@@ -47,6 +54,11 @@ __global__ void mlp_node_features(NodeView nv, EnvView ev, __nv_bfloat16 *feat) 
       s[k++] = angle ? wrap_pi_f64(x[i]) * 0.31830988618f : (float)(x[i] / 4.0);
     }
   }
+  if (gv.has)
+    for (int i = 0; i < R::POSD; i++) {
+      const double ext = ev.hi[i] - ev.lo[i];
+      s[13 + i] = ext > 0 ? (float)(2.0 * (gv.g[i] - x[i]) / ext) : 0.f;
+    }
 #pragma unroll
   for (int i = 0; i < 16; i++) f[i] = __float2bfloat16_rn(s[i]);
   const float px = (float)x[0], py = (float)x[1];
@@ -100,13 +112,18 @@ static __global__ void mlp_loss(const float *out, const float *target, int64_t B
     __align__(16) __nv_bfloat16 row[64];
 #pragma unroll
     for (int j = 0; j < 64; j++) row[j] = __float2bfloat16_rn(0.f);
-    if (b < B) {
+    if (b < B) {  // a NaN target leaves its head out of the loss
       const float lg = out[b * 2], ct = out[b * 2 + 1];
       const float y = target[b * 2], t = target[b * 2 + 1];
-      l = softplus(lg) - y * lg + 0.5f * ctg_weight * (ct - t) * (ct - t);
       const float inv = 1.f / (float)B;
-      row[0] = __float2bfloat16_rn((sigmoid(lg) - y) * inv);
-      row[1] = __float2bfloat16_rn(ctg_weight * (ct - t) * inv);
+      if (!isnan(y)) {
+        l += softplus(lg) - y * lg;
+        row[0] = __float2bfloat16_rn((sigmoid(lg) - y) * inv);
+      }
+      if (!isnan(t)) {
+        l += 0.5f * ctg_weight * (ct - t) * (ct - t);
+        row[1] = __float2bfloat16_rn(ctg_weight * (ct - t) * inv);
+      }
     }
     uint4 *dst = reinterpret_cast<uint4 *>(dY + b * 64);
 #pragma unroll

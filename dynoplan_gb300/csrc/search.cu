@@ -19,6 +19,8 @@ using namespace dpg;
 
 namespace {
 
+// the surrogate's cost-to-go output is in units of this many seconds
+constexpr double kCtgScale = 10.0;
 constexpr double kTwoPiH = 6.283185307179586476925286766559;
 constexpr double kPiH = 3.1415926535897932384626433832795;
 
@@ -441,6 +443,29 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       return DPG_ERR_CUDA;
     res->novelty_ms += elapsed_ms() - tn0;
 
+    // learned heuristic: the surrogate's cost-to-go of every (node, motion)
+    // candidate, never below the time lower bound
+    std::vector<float> pred;
+    if (o->heuristic == DPG_HEU_MLP) {
+      const double tm0 = elapsed_ms();
+      std::vector<uint32_t> cn(Q), cp(Q);
+      for (int i = 0; i < Q; i++) {
+        cn[i] = (uint32_t)cands[i].batch_node;
+        cp[i] = (uint32_t)cands[i].prim;
+      }
+      if (!b64.reserve((size_t)B * nx) || !feat.reserve((size_t)B * kMlpNodeFeat) || !pnode.reserve(Q) ||
+          !pprim.reserve(Q) || !mlp_out.reserve((size_t)Q * 2))
+        return DPG_ERR_OOM;
+      cudaMemcpy(b64.p, bx.data(), sizeof(double) * bx.size(), cudaMemcpyHostToDevice);
+      cudaMemcpy(pnode.p, cn.data(), sizeof(uint32_t) * Q, cudaMemcpyHostToDevice);
+      cudaMemcpy(pprim.p, cp.data(), sizeof(uint32_t) * Q, cudaMemcpyHostToDevice);
+      if ((rc = dpg_mlp_node_features(c, b64.p, B, goal, feat.p))) return rc;
+      if ((rc = dpg_mlp_forward(mlp, feat.p, pnode.p, pprim.p, Q, mlp_out.p))) return rc;
+      pred.resize((size_t)Q * 2);
+      cudaMemcpy(pred.data(), mlp_out.p, sizeof(float) * Q * 2, cudaMemcpyDeviceToHost);
+      res->mlp_ms += elapsed_ms() - tm0;
+    }
+
     // insert or rewire, in pop order and the candidates' order (dbastar.cpp:809-919)
     std::vector<int> accepted_as(Q, -1);  // node id of an accepted candidate
     for (int b = 0; b < B; b++) {
@@ -448,7 +473,8 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       int n_new = 0;
       for (int ci = first_cand[b]; ci < first_cand[b + 1]; ci++) {
         Cand &cd = cands[ci];
-        const double h = (o->heuristic == DPG_HEU_BLIND) ? 0.0 : lower_bound_time(r, cd.x.data(), goal);
+        double h = (o->heuristic == DPG_HEU_BLIND) ? 0.0 : lower_bound_time(r, cd.x.data(), goal);
+        if (o->heuristic == DPG_HEU_MLP) h = std::max(h, kCtgScale * std::max(0.0, (double)pred[2 * (size_t)ci + 1]));
         const double g = (double)nodes[parent].g + cd.cost +
                          o->cost_delta_factor * lower_bound_time(r, &xs[(size_t)parent * nx], cd.x0.data());
         std::vector<int> nbr;

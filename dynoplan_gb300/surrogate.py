@@ -81,12 +81,15 @@ class Surrogate:
         return ms.value, fl.value
 
 
-def node_features(ctx, x_dev):
-    """[N x 80] bf16 node features (state + occupancy) for the context's env"""
+def node_features(ctx, x_dev, goal=None):
+    """[N x 80] bf16 node features (state + occupancy, and the offset to
+    `goal` when given) for the context's env"""
     import torch
     N = x_dev.shape[0]
     feat = torch.empty((N, NODE_FEAT), dtype=torch.bfloat16, device=x_dev.device)
-    check(_lib.load().dpg_mlp_node_features(ctx.h, _p(x_dev), N, _p(feat)), ctx.h)
+    g = None if goal is None else np.ascontiguousarray(goal, dtype=np.float64)
+    check(_lib.load().dpg_mlp_node_features(ctx.h, _p(x_dev), N, g.ctypes.data if g is not None else None,
+                                            _p(feat)), ctx.h)
     return feat
 
 
@@ -145,6 +148,55 @@ def make_dataset(wl, n_envs: int, nodes_per_env: int, pairs_per_env: int, seed: 
                    torch.from_numpy(np.concatenate(nodes_g).astype(np.int32)).to(dev),
                    torch.from_numpy(np.concatenate(prims).astype(np.int32)).to(dev),
                    torch.from_numpy(np.concatenate(targets)).to(dev), n_envs, np.concatenate(env_of))
+
+
+def search_dataset(robot, prims, problems, opts, nodes_per_env: int = 600, radius: float | None = None,
+                   device: int = 0, log=None):
+    """Labels from completed searches and the exact checker, goal-conditioned:
+      - every (node, motion) pair on a solution path of a plain search, with
+        the remaining cost from its successor to the goal as cost-to-go and
+        collision 0;
+      - every in-ball pair of `nodes_per_env` free nodes, exact-checked, with
+        its collision label (no cost-to-go: NaN).
+    problems: list of (env, start, goal).  Returns (Dataset, search results)."""
+    import torch
+
+    from . import gpu as G
+    from . import search as S
+    radius = radius if radius is not None else opts.alpha * opts.delta
+    feats, nodes_g, prims_l, targets, results = [], [], [], [], []
+    base = 0
+    dev = f"cuda:{device}"
+    with G.Context(robot, device=device) as ctx:
+        ctx.upload_primitives(prims)
+        for i, (env, start, goal) in enumerate(problems):
+            ctx.upload_env(env)
+            res, motions, states = S.search(ctx, start, goal, opts)
+            results.append(res)
+            rand = W.make_nodes(robot, env, nodes_per_env, seed=7000 + i, vel_sigma=0.5)
+            node_states = np.concatenate([states[:-1], rand], 0) if res["solved"] else rand
+            x_dev = torch.from_numpy(np.ascontiguousarray(node_states)).to(dev)
+            feats.append(node_features(ctx, x_dev, goal))
+            n_path = len(motions) if res["solved"] else 0
+            if n_path:
+                cost = np.array([(int(prims.length[p]) - 1) * robot.dt for p in motions])
+                remaining = cost[::-1].cumsum()[::-1] - cost   # after motion i
+                nodes_g.append(np.arange(n_path) + base)
+                prims_l.append(motions.astype(np.int64))
+                targets.append(np.stack([np.zeros(n_path), remaining / CTG_SCALE], 1).astype(np.float32))
+            exp = ctx.expand(rand, radius, precision=0)
+            nodes_g.append(exp["node"].astype(np.int64) + n_path + base)
+            prims_l.append(exp["prim"].astype(np.int64))
+            targets.append(np.stack([(exp["verdict"] != 0).astype(np.float32),
+                                     np.full(exp["n_pairs"], np.nan, np.float32)], 1))
+            base += len(node_states)
+            if log:
+                log(f"problem {i}: {res['status_str']} cost {res['cost']:.2f} in {res['time_ms']:.0f} ms")
+    ds = Dataset(torch.cat(feats, 0).contiguous(),
+                 torch.from_numpy(np.concatenate(nodes_g).astype(np.int32)).to(dev),
+                 torch.from_numpy(np.concatenate(prims_l).astype(np.int32)).to(dev),
+                 torch.from_numpy(np.concatenate(targets)).to(dev), len(problems), None)
+    return ds, results
 
 
 def train(model: Surrogate, ds: Dataset, epochs: float, batch: int = 65536, lr: float = 2e-3, seed: int = 0,

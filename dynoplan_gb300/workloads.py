@@ -244,6 +244,62 @@ def make_primitives(m: RobotModel, P: int, steps_lo: int, steps_hi: int, seed: i
     return Primitives(length, np.ascontiguousarray(states), np.ascontiguousarray(actions))
 
 
+def make_primitives_hover(m: RobotModel, P: int, steps_lo: int, steps_hi: int, seed: int, hold: int = 20,
+                          tilt: float = 0.3, rate: float = 1.0, lift: tuple = (0.8, 1.25),
+                          kp: float = 16.0, kd: float = 5.6, noise: float = 1e-7) -> Primitives:
+    """quad2d motions that chain: canonical starts with |theta| <= tilt,
+    |omega| <= rate and zero velocity; every `hold` steps a new tilt target in
+    [-tilt, tilt] and lift factor in `lift` are drawn and a PD law on the
+    angle (kp, kd in rad/s^2 per rad, per rad/s) sets the thrust difference,
+    so the motion ends near level again.  The applied thrusts, clipped to
+    the actuator bounds, are recorded as the motion's actions; then the
+    loader's 1e-7 noise."""
+    rng = Rng(seed)
+    steps = rng.integers(P, steps_lo, steps_hi)
+    x0 = np.zeros((P, m.nx))
+    x0[:, 2] = rng.uniform(P, -tilt, tilt)
+    x0[:, 5] = rng.uniform(P, -rate, rate)
+    T = int(steps.max())
+    n_hold = (T + hold - 1) // hold
+    ref = rng.uniform((P, n_hold), -tilt, tilt)
+    c = rng.uniform((P, n_hold), lift[0], lift[1])
+    lb, ub = np.array(m.u_lb), np.array(m.u_ub)
+    gain = m.ang_gain * m.g * 0.5
+    X = np.empty((P, T + 1, m.nx))
+    U = np.empty((P, T, m.nu))
+    X[:, 0] = x0
+    for k in range(T):
+        j = k // hold
+        th, om = X[:, k, 2], X[:, k, 5]
+        d = (kp * (ref[:, j] - th) - kd * om) / gain
+        base = c[:, j] / np.maximum(np.cos(th), 0.5)
+        U[:, k] = np.clip(np.stack([base + 0.5 * d, base - 0.5 * d], 1), lb, ub)
+        X[:, k + 1] = step(m, X[:, k], U[:, k])
+    length = (steps + 1).astype(np.int32)
+    X[:, 0] += noise * rng.uniform((P, m.nx), -1.0, 1.0)
+    X[np.arange(P), steps] += noise * rng.uniform((P, m.nx), -1.0, 1.0)
+    states = np.concatenate([X[p, :length[p]] for p in range(P)], 0)
+    actions = np.concatenate([U[p, :length[p] - 1] for p in range(P)], 0)
+    return Primitives(length, np.ascontiguousarray(states), np.ascontiguousarray(actions))
+
+
+def make_search_problem(m: RobotModel, extent, n_obs_range, side, seed: int, margin: float = 0.05):
+    """Environment with a random number of boxes in n_obs_range, and a start
+    and a goal at rest (level, zero velocity) in free space."""
+    rng = Rng(seed)
+    n_obs = int(rng.integers(1, n_obs_range[0], n_obs_range[1])[0])
+    env = make_env(extent, n_obs, side[0], side[1], seed + 1)
+    out = []
+    s = seed + 2
+    while len(out) < 2:
+        x = make_nodes(m, env, 8, seed=s, vel_sigma=0.0)
+        s += 1
+        x[:, 2:] = 0.0
+        ok = state_gap(m, env, x) > margin
+        out.extend(x[ok][: 2 - len(out)])
+    return env, np.array(out[0]), np.array(out[1])
+
+
 # ------------------------------------------------------------- environment --
 
 @dataclasses.dataclass
@@ -355,7 +411,8 @@ CONFIGS = {
     3: dict(name="quadrotor_v0 batched FP32 expand", kind=QUAD3D, P=5000, steps=(50, 300),
             extent=(6.0, 6.0, 3.0), n_obs=40, side=(0.2, 1.0), N=50_000, delta=0.8, precision=0),
     5: dict(name="quad2d_v0 end-to-end", kind=QUAD2D, P=10_000, steps=(20, 150),
-            extent=(8.0, 4.0), n_obs=40, side=(0.2, 1.0), N=10_000, delta=0.5, precision=0),
+            extent=(8.0, 4.0), n_obs=40, side=(0.2, 1.0), N=10_000, delta=0.5, precision=0,
+            n_obs_range=(20, 60)),
 }
 
 

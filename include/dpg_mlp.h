@@ -53,8 +53,10 @@ int dpg_mlp_get(const dpg_mlp *mlp, int which, int grad, float *host);
 int dpg_mlp_set(dpg_mlp *mlp, int which, const float *host);
 
 /* per node: normalised state + occupancy patch (80 bf16 per node) from the
- * context's environment; x_dev N x nx doubles */
-int dpg_mlp_node_features(dpg_ctx *ctx, const double *x_dev, int64_t N, void *feat_dev);
+ * context's environment; x_dev N x nx doubles.  goal (host, nx doubles, may
+ * be NULL): the goal the cost-to-go refers to, stored as the normalised
+ * offset goal - position in state slots 13.. */
+int dpg_mlp_node_features(dpg_ctx *ctx, const double *x_dev, int64_t N, const double *goal, void *feat_dev);
 
 /* scores n pairs: out_dev[n x 2] = [logit, cost-to-go] (FP32) */
 int dpg_mlp_forward(dpg_mlp *mlp, const void *node_feat_dev, const uint32_t *node_dev, const uint32_t *prim_dev,
