@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--nodes", type=int, default=None, help="frontier states per step (default: the workload's)")
+    ap.add_argument("--envs", type=int, default=200, help="--config 4: training environments")
+    ap.add_argument("--problems", type=int, default=100, help="--config 5: evaluation problems")
+    ap.add_argument("--train-problems", type=int, default=64, help="--config 5: problems the heuristic learns from")
     return ap.parse_args()
 
 
@@ -443,6 +446,219 @@ def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
     return e2e, list(hosts.values()) + [xh]
 
 
+# ------------------------------------------------- surrogate (car1_v0 MLP) --
+MLP_IN_USED = 96      # 80 node features + 16 primitive embedding (the rest of the 128 is padding)
+MLP_HIDDEN = 256
+MLP_OUT_USED = 2      # collision logit, cost-to-go
+# assemble, 4 forward GEMMs, loss, 4 x (2 transposes, dW GEMM, column sums,
+# dX GEMM), 9 Adam updates, 4 x (bf16 copy, transpose) + embedding copy
+MLP_KERNELS_PER_TRAIN_STEP = 44
+
+
+def mlp_alg_flops(rows):
+    """forward FLOPs of the layers' used widths: 96 -> 256 -> 256 -> 256 -> 2"""
+    return 2.0 * rows * (MLP_IN_USED * MLP_HIDDEN + 2 * MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN * MLP_OUT_USED)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "hbm_gbs": 6800.0}, "fallback"
+
+
+def lazy_check_counts(node, valid, score, limit=20):
+    """Exact checks a lazy loop needs per node to find `limit` valid motions:
+    in motion order (the reference) and in ascending predicted-collision
+    order; nodes with fewer valid motions check all of theirs."""
+    ref = mlp = 0
+    order = np.lexsort((score, node))
+    for sel_order, acc in ((np.lexsort((np.arange(len(node)), node)), "ref"), (order, "mlp")):
+        n_s, v_s = node[sel_order], valid[sel_order]
+        starts = np.flatnonzero(np.r_[True, n_s[1:] != n_s[:-1]])
+        ends = np.r_[starts[1:], len(n_s)]
+        total = 0
+        for s, e in zip(starts, ends):
+            c = np.cumsum(v_s[s:e])
+            hit = np.searchsorted(c, limit)
+            total += (hit + 1) if hit < e - s else (e - s)
+        if acc == "ref":
+            ref = total
+        else:
+            mlp = total
+    return ref, mlp
+
+
+def run_surrogate(args, rank, world, local_rank):
+    """The learned surrogate on car1_v0: BF16 tcgen05 training steps (batch
+    65,536) on exact labels of the car1 workload's primitives in seeded
+    environments; then inference and label quality on held-out environments."""
+    import torch
+
+    from dynoplan_gb300 import _lib
+    from dynoplan_gb300 import surrogate as SG
+    from dynoplan_gb300 import workloads as W
+    if rank > 0:
+        return
+    lib = _lib.load()
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    wl = W.make_workload(2)
+    batch = 65536
+    t0 = time.perf_counter()
+    ds = SG.make_dataset(wl, n_envs=args.envs, nodes_per_env=700, pairs_per_env=50000, seed=4, device=dev)
+    held = SG.make_dataset(wl, n_envs=8, nodes_per_env=2000, pairs_per_env=10 ** 6, seed=5, device=dev)
+    build_s = time.perf_counter() - t0
+    model = SG.Surrogate(wl.prims.P, max_rows=1 << 20, device=dev, seed=0)
+    g = torch.Generator(device=ds.node.device).manual_seed(0)
+    n = len(ds)
+
+    def step(i, lr):
+        idx = torch.randint(0, n, (batch,), generator=g, device=ds.node.device)
+        loss = model.train_step(ds.node_feat, ds.node[idx].contiguous(), ds.prim[idx].contiguous(),
+                                ds.target[idx].contiguous(), lr=lr)
+        return loss, model.timing()[0]
+
+    for i in range(args.warmup):
+        step(i, 2e-3)
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    ms = []
+    losses = []
+    for i in range(args.steps):
+        lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
+        loss, t = step(i, 2e-3)
+        ms.append(t)
+        losses.append(loss)
+    clk = clocks.stop()
+    train_s = sum(ms) * 1e-3
+    value = args.steps * batch / train_s
+    peaks, src = measured_peaks()
+    achieved = 3 * mlp_alg_flops(batch) * args.steps / train_s / 1e12
+    # a quality pass: train on to ~3 epochs before the held-out metrics
+    extra = max(0, int(3 * n / batch) - args.steps - args.warmup)
+    for i in range(extra):
+        step(i, 2e-3 * 0.5 * (1 + np.cos(np.pi * i / max(extra, 1))))
+    # inference: one launch over up to 2^20 held-out pairs
+    m = min(len(held), 1 << 20)
+    node_h, prim_h = held.node[:m].contiguous(), held.prim[:m].contiguous()
+    out = model.forward(held.node_feat, node_h, prim_h)
+    inf_ms = []
+    for _ in range(5):
+        lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
+        model.forward(held.node_feat, node_h, prim_h, out)
+        inf_ms.append(model.timing()[0])
+    inf_s = statistics.median(inf_ms) * 1e-3
+    logit = out[:, 0].float().cpu().numpy()
+    y = held.target[:m, 0].cpu().numpy() > 0.5
+    pred = logit > 0
+    tp = int((pred & y).sum())
+    precision = tp / max(int(pred.sum()), 1)
+    recall = tp / max(int(y.sum()), 1)
+    ref_checks, mlp_checks = lazy_check_counts(node_h.cpu().numpy(), (~y).astype(np.int64), logit)
+    line = {
+        "metric": "surrogate training samples/s", "value": value, "unit": "samples/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * train_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic (seeded car1_v0 environments, exact GPU labels)",
+        "config": {"workload": "car1_v0 surrogate", "batch": batch, "labels": n, "envs": args.envs,
+                   "layers": "128(96 used)->256->256->256->16(2 used), GELU, Adam",
+                   "dataset_build_s": build_s, "l2": "flushed between steps"},
+        "roofline": {"bound": "tensor", "kernel": "train step (tcgen05 GEMMs + epilogues)", "achieved": achieved,
+                     "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                     "frac": achieved / peaks["bf16_tflops_sustained"], "traffic": None,
+                     "peak_source": f"{src} bf16 sustained",
+                     "work_model": "3 x forward FLOPs of the used widths per sample"},
+        "inference": {"pairs": m, "ms": 1e3 * inf_s, "pairs_per_s": m / inf_s,
+                      "tflops": mlp_alg_flops(m) / inf_s / 1e12,
+                      "frac": mlp_alg_flops(m) / inf_s / 1e12 / peaks["bf16_tflops"]},
+        "quality": {"held_out_pairs": m, "collision_rate": float(y.mean()), "precision": precision,
+                    "recall": recall, "loss_last": losses[-1],
+                    "lazy_checks_for_20_valid": {"motion_order": ref_checks, "mlp_order": mlp_checks}},
+        "gpu_launches": MLP_KERNELS_PER_TRAIN_STEP * args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------- end-to-end search (quad2d) --
+def run_search(args, rank, world, local_rank):
+    """db-A* on quad2d_v0 problems (8 x 4 m, 20-60 boxes, start and goal at
+    rest in free space), 10,000 primitives of 20-150 steps: the plain time
+    lower-bound heuristic against the learned cost-to-go (trained first on
+    separate problems from completed plain searches).  Reports
+    time-to-first-solution and cost per heuristic."""
+    import torch
+
+    from dynoplan_gb300 import gpu as G
+    from dynoplan_gb300 import search as S
+    from dynoplan_gb300 import surrogate as SG
+    from dynoplan_gb300 import workloads as W
+    if rank > 0:
+        return
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    m = W.robot_model(W.QUAD2D)
+    prims = W.make_primitives_hover(m, 10000, 20, 150, seed=1005)
+    problem = lambda i: W.make_search_problem(m, (8.0, 4.0), (20, 60), (0.2, 1.0), seed=1005 + 17 * i)
+    train_probs = [problem(i) for i in range(args.problems, args.problems + args.train_problems)]
+    eval_probs = [problem(i) for i in range(args.problems)]
+    delta, batch, limit_ms = 0.5, 32, 5000.0
+    t0 = time.perf_counter()
+    ds, tr = SG.search_dataset(m, prims, train_probs,
+                               S.options(delta, batch=batch, max_expands=10 ** 6, time_limit_ms=limit_ms),
+                               device=dev)
+    model = SG.Surrogate(prims.P, max_rows=65536, device=dev, seed=0)
+    _, train_sps, train_tf = SG.train(model, ds, epochs=8, batch=16384, lr=2e-3)
+    setup_s = time.perf_counter() - t0
+    clocks = Clocks(dev)
+    rows = {}
+    with G.Context(m, device=dev) as ctx:
+        ctx.upload_primitives(prims)
+        for name, heu in (("plain", S.HEU_EUCLIDEAN), ("mlp", S.HEU_MLP)):
+            opts = S.options(delta, batch=batch, heuristic=heu, max_expands=10 ** 6, time_limit_ms=limit_ms)
+            rows[name] = []
+            for env, s, g in eval_probs:
+                ctx.upload_env(env)
+                r, _, _ = S.search(ctx, s, g, opts, mlp=model if heu == S.HEU_MLP else None)
+                rows[name].append(r)
+    clk = clocks.stop()
+
+    def summary(rs):
+        solved = [r for r in rs if r["solved"]]
+        t = [r["time_ms"] for r in solved]
+        return {"solved": len(solved), "of": len(rs),
+                "median_time_ms": statistics.median(t) if t else None,
+                "mean_time_ms": statistics.mean(t) if t else None,
+                "median_cost_s": statistics.median([r["cost"] for r in solved]) if solved else None,
+                "expands": int(sum(r["expands"] for r in rs)), "checked_pairs": int(sum(r["checked_pairs"] for r in rs)),
+                "expand_ms": sum(r["expand_ms"] for r in rs), "novelty_ms": sum(r["novelty_ms"] for r in rs),
+                "mlp_ms": sum(r["mlp_ms"] for r in rs), "total_ms": sum(r["time_ms"] for r in rs)}
+    both = [i for i in range(len(eval_probs)) if rows["plain"][i]["solved"] and rows["mlp"][i]["solved"]]
+    ratio = [rows["plain"][i]["time_ms"] / max(rows["mlp"][i]["time_ms"], 1e-3) for i in both]
+    cost_ratio = [rows["mlp"][i]["cost"] / max(rows["plain"][i]["cost"], 1e-9) for i in both]
+    plain = summary(rows["plain"])
+    line = {
+        "metric": "db-A* time to first solution (median over solved problems, plain heuristic)",
+        "value": plain["median_time_ms"], "unit": "ms", "n_gpus": 1, "steps": len(eval_probs), "warmup": 0,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded quad2d_v0 problems, hover-chaining primitives)",
+        "config": {"workload": "quad2d_v0 end-to-end", "primitives": prims.P, "steps_per_primitive": [20, 150],
+                   "env": "8 x 4 m, 20-60 boxes of 0.2-1.0 m", "delta": delta, "alpha": 0.5,
+                   "batch": batch, "time_limit_ms": limit_ms, "train_problems": len(train_probs),
+                   "train_solved": int(sum(r["solved"] for r in tr)), "train_labels": len(ds),
+                   "setup_s": setup_s, "train_samples_per_s": train_sps, "train_tflops": train_tf},
+        "plain": plain, "mlp": summary(rows["mlp"]),
+        "both_solved": len(both),
+        "median_speedup_mlp": statistics.median(ratio) if ratio else None,
+        "geomean_speedup_mlp": float(np.exp(np.mean(np.log(ratio)))) if ratio else None,
+        "median_cost_ratio_mlp": statistics.median(cost_ratio) if cost_ratio else None,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_peak(lib, dev):
     import ctypes as C
     v = C.c_double()
@@ -455,6 +671,10 @@ def main():
     rank, world, local_rank = dist_info()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.config == 4:
+        run_surrogate(args, rank, world, local_rank)
+    elif args.config == 5:
+        run_search(args, rank, world, local_rank)
     else:
         run_ours(args, rank, world, local_rank)
 

@@ -109,6 +109,15 @@ template <class F> void with_kind(int kind, F &&f) {
 
 }  // namespace
 
+// primitive tiles per nn_mask block: small node batches are split over the
+// primitives too, for about two blocks per SM
+static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
+  const int ntiles = std::max(1, (P + kNNTile - 1) / kNNTile);
+  const int64_t want = std::max<int64_t>(1, (2 * (int64_t)sm_count + B - 1) / std::max<int64_t>(B, 1));
+  const int y = (int)std::min<int64_t>(ntiles, want);
+  return (ntiles + y - 1) / y;
+}
+
 extern "C" {
 
 int dpg_abi_version(void) { return DPG_ABI_VERSION; }
@@ -181,7 +190,9 @@ int dpg_create(dpg_ctx **out, int device, const dpg_robot_desc *robot) {
     if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
       rc = DPG_ERR_NODEVICE; break;
     }
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = DPG_ERR_CUDA; break; }
+    // a blocking stream: ordered after the caller's work on the legacy
+    // default stream, which produces device-resident inputs
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamDefault) != cudaSuccess) { rc = DPG_ERR_CUDA; break; }
     if (cudaMalloc(&c->d_ctr, sizeof(DevCounters)) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
     if (cudaHostAlloc(&c->h_ctr, sizeof(DevCounters), cudaHostAllocDefault) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
     if (cudaHostAlloc(&c->h_abort, sizeof(int), cudaHostAllocMapped) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
@@ -495,9 +506,10 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
       const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
-      nn_mask<KIND><<<(unsigned)B, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)opts->radius, opts->radius,
-                                                       (float)ball_band, Ppad, P_<uint32_t>(c->mask),
-                                                       P_<uint32_t>(c->cnt), ctr);
+      const int tpy = nn_tiles_per_y(P, B, c->sm_count);
+      const dim3 ng((unsigned)B, (unsigned)((P + tpy * kNNTile - 1) / (tpy * kNNTile)));
+      nn_mask<KIND><<<ng, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)opts->radius, opts->radius, (float)ball_band,
+                                               Ppad, tpy, P_<uint32_t>(c->mask), P_<uint32_t>(c->cnt), ctr);
       nn_prefix<<<(P + 255) / 256, 256, 0, st>>>(P, (int)B, P_<uint32_t>(c->cnt), P_<uint32_t>(c->tot));
     } else {
       cudaMemsetAsync(c->tot.p, 0, sizeof(uint32_t) * P, st);
@@ -735,8 +747,10 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
       const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
-      nn_mask<KIND><<<(unsigned)B, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)opts->radius, opts->radius,
-                                                       (float)ball_band, Ppad, mask, cnt, ctr);
+      const int tpy = nn_tiles_per_y(P, B, c->sm_count);
+      const dim3 ng((unsigned)B, (unsigned)((P + tpy * kNNTile - 1) / (tpy * kNNTile)));
+      nn_mask<KIND><<<ng, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)opts->radius, opts->radius, (float)ball_band,
+                                               Ppad, tpy, mask, cnt, ctr);
       nn_prefix<<<(P + 255) / 256, 256, 0, st>>>(P, (int)B, cnt, tot);
     } else {
       cudaMemsetAsync(tot, 0, sizeof(uint32_t) * P, st);

@@ -150,13 +150,15 @@ __device__ __forceinline__ float key_dist32(const float4 w, const float *nk,
   }
 }
 
-// Ball membership of 256 nodes (one block) against all primitives.
+// Ball membership of 256 nodes (blockIdx.x) against the primitives of
+// `tiles_per_y` tiles of kNNTile (blockIdx.y), so that small node batches
+// still fill the GPU.
 // mask[w * Ppad + p] bit l  <=>  node 32 w + l is within radius of prim p.
 // cnt[b * P + p] = members of prim p among the block's nodes.
 template <int KIND>
 __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView pv, NodeView nv,
                                                       float4 w32, float radius, double radius64, float band, int Ppad,
-                                                      uint32_t *mask, uint32_t *cnt,
+                                                      int tiles_per_y, uint32_t *mask, uint32_t *cnt,
                                                       DevCounters *ctr) {
   using R = Robot<KIND>;
   __shared__ float sk[R::KEYD * kNNTile];
@@ -171,7 +173,9 @@ __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView p
   for (int i = 0; i < R::KEYD; i++) nk[i] = live ? nv.key32[i * nv.N + n] : 0.f;
   unsigned long long rechecks = 0;
 
-  for (int p0 = 0; p0 < pv.P; p0 += kNNTile) {
+  const int p_begin = blockIdx.y * tiles_per_y * kNNTile;
+  const int p_end = min(pv.P, p_begin + tiles_per_y * kNNTile);
+  for (int p0 = p_begin; p0 < p_end; p0 += kNNTile) {
     const int tp = min(kNNTile, pv.P - p0);
     __syncthreads();
     for (int t = threadIdx.x; t < tp; t += blockDim.x) {

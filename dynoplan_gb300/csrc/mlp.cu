@@ -194,7 +194,8 @@ int dpg_mlp_create(dpg_mlp **out, int device, int n_prims, int64_t max_rows, uin
   const int64_t sizes[DPG_MLP_NPARAM] = {(int64_t)kMlpHidden * kMlpIn, kMlpHidden, (int64_t)kMlpHidden * kMlpHidden,
                                          kMlpHidden, (int64_t)kMlpHidden * kMlpHidden, kMlpHidden,
                                          (int64_t)kMlpOutPad * kMlpHidden, kMlpOutPad, (int64_t)n_prims * kMlpEmb};
-  bool ok = cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking) == cudaSuccess;
+  // blocking: ordered after the caller's legacy-default-stream work
+  bool ok = cudaStreamCreateWithFlags(&M->stream, cudaStreamDefault) == cudaSuccess;
   for (int i = 0; i < DPG_MLP_NPARAM && ok; i++) {
     M->n[i] = sizes[i];
     ok = dalloc(&M->w[i], sizes[i]) == cudaSuccess && dalloc(&M->g[i], sizes[i]) == cudaSuccess &&

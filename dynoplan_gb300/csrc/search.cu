@@ -223,15 +223,6 @@ template <class T> struct DVec {  // growable device array
   }
 };
 
-struct Cand {
-  int batch_node;   // index into the batch
-  int prim;
-  int chosen;       // intermediate state index (check_goal) or -1
-  double cost;      // motion duration
-  std::vector<double> x;  // successor state
-  std::vector<double> x0; // transformed start of the motion
-};
-
 }  // namespace
 
 int dpg_ctx_host_states(dpg_ctx *c, std::vector<double> &out) {
@@ -262,7 +253,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   if (rc) return rc;
   const double goal_tol = o->delta_factor_goal * o->delta;
   const double nov_radius = (1.0 - o->alpha) * o->delta;
-  const int K = std::max(1, o->max_neighbors);
+  int Kq = std::max(1, o->max_neighbors);  // neighbour-id capacity per query
   std::mt19937 rng((uint32_t)o->seed);
 
   // explored nodes (host) + their states mirrored on the GPU for the queries
@@ -346,7 +337,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
     const int B = (int)batch.size();
     std::vector<double> bx((size_t)B * nx);
     for (int i = 0; i < B; i++) std::memcpy(&bx[(size_t)i * nx], &xs[(size_t)batch[i] * nx], sizeof(double) * nx);
-    int64_t cap = std::max<int64_t>(1024, (int64_t)B * 256);
+    int64_t cap = std::max<int64_t>(1024, (int64_t)B * P);  // every pair of the batch
     dpg_expand_out eo{};
     dpg_expand_opts eopt{};
     eopt.radius = o->alpha * o->delta;
@@ -367,153 +358,179 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
     res->expand_ms += elapsed_ms() - te0;
     res->checked_pairs += eo.n_pairs;
 
-    // candidates per batch node, valid pairs, in expand_lazy's order
+    // valid motions per batch node, in expand_lazy's order
     std::vector<std::vector<int>> per_node(B);
     for (int64_t i = 0; i < eo.n_pairs; i++)
       if (h_verdict[i] == DPG_VALID) per_node[h_node[i]].push_back((int)h_prim[i]);
-    std::vector<Cand> cands;
-    std::vector<int> first_cand(B + 1, 0);
     for (int b = 0; b < B; b++) {
-      auto &v = per_node[b];
-      std::sort(v.begin(), v.end());
-      if (o->shuffle) std::shuffle(v.begin(), v.end(), rng);
-      first_cand[b] = (int)cands.size();
-      const double *x = &bx[(size_t)b * nx];
-      for (int p : v) {
-        Cand cd;
-        cd.batch_node = b;
-        cd.prim = p;
-        const int L = c->h_len[p];
-        cd.x.resize(nx);
-        cd.x0.resize(nx);
-        transformed_state(r, st, c->h_soff[p], L - 1, x, cd.x.data());
-        transformed_state(r, st, c->h_soff[p], 0, x, cd.x0.data());
-        cd.chosen = -1;
-        // check_goal: states at floor((k+1)/(n+1) * L), k = 0..3 (dbastar.cpp:492-512)
-        std::vector<double> xi(nx);
-        for (int k = 0; k < 4; k++) {
-          const int idx = (int)((float)(k + 1) / 5.0f * (float)L);
-          if (idx >= L) continue;
-          transformed_state(r, st, c->h_soff[p], idx, x, xi.data());
-          if (distance(r, xi.data(), goal) <= goal_tol) {
-            cd.x = xi;
-            cd.chosen = idx;
-            break;
-          }
-        }
-        cd.cost = (cd.chosen != -1 ? cd.chosen : L - 1) * r.dt;
-        cands.push_back(std::move(cd));
-      }
+      std::sort(per_node[b].begin(), per_node[b].end());
+      if (o->shuffle) std::shuffle(per_node[b].begin(), per_node[b].end(), rng);
     }
-    first_cand[B] = (int)cands.size();
-    const int Q = (int)cands.size();
-    if (Q == 0) continue;
-
-    // novelty: candidates vs explored nodes, and vs earlier candidates
-    const double tn0 = elapsed_ms();
-    if (!sync_table() || !q64.reserve((size_t)Q * nx) || !q32.reserve((size_t)Q * nx) ||
-        !cnt_tab.reserve(Q) || !ids_tab.reserve((size_t)Q * K) || !cnt_self.reserve(Q) ||
-        !ids_self.reserve((size_t)Q * K))
-      return DPG_ERR_OOM;
-    std::vector<double> qh((size_t)Q * nx);
-    for (int i = 0; i < Q; i++) std::memcpy(&qh[(size_t)i * nx], cands[i].x.data(), sizeof(double) * nx);
-    std::vector<float> qf(qh.begin(), qh.end());
-    cudaMemcpy(q64.p, qh.data(), sizeof(double) * qh.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(q32.p, qf.data(), sizeof(float) * qf.size(), cudaMemcpyHostToDevice);
-    cudaMemset(cnt_tab.p, 0, sizeof(int) * Q);
-    cudaMemset(cnt_self.p, 0, sizeof(int) * Q);
-    const int T = (int)nodes.size();
-    with_kind_s(r.kind, [&](auto Kd) {
-      constexpr int KIND = decltype(Kd)::value;
-      for (int q0 = 0; q0 < Q; q0 += 65535) {  // grid.y limit
-        const int nq = std::min(65535, Q - q0);
-        dim3 g1((unsigned)std::min(64, (T + 255) / 256), (unsigned)nq);
-        radius_query<KIND><<<g1, 256>>>(c->rp, w32, q64.p, q32.p, Q, q0, t64.p, t32.p, T, nov_radius, 1e-5f, 0, K,
-                                        cnt_tab.p, ids_tab.p);
-        dim3 g2((unsigned)std::min(64, (Q + 255) / 256), (unsigned)nq);
-        radius_query<KIND><<<g2, 256>>>(c->rp, w32, q64.p, q32.p, Q, q0, q64.p, q32.p, Q, nov_radius, 1e-5f, 1, K,
-                                        cnt_self.p, ids_self.p);
-      }
-    });
-    std::vector<int> ct(Q), it((size_t)Q * K), cs(Q), is((size_t)Q * K);
-    cudaMemcpy(ct.data(), cnt_tab.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
-    cudaMemcpy(it.data(), ids_tab.p, sizeof(int) * Q * K, cudaMemcpyDeviceToHost);
-    cudaMemcpy(cs.data(), cnt_self.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
-    if (cudaMemcpy(is.data(), ids_self.p, sizeof(int) * Q * K, cudaMemcpyDeviceToHost) != cudaSuccess)
-      return DPG_ERR_CUDA;
-    res->novelty_ms += elapsed_ms() - tn0;
-
-    // learned heuristic: the surrogate's cost-to-go of every (node, motion)
-    // candidate, never below the time lower bound
-    std::vector<float> pred;
-    if (o->heuristic == DPG_HEU_MLP) {
+    if (o->heuristic == DPG_HEU_MLP) {  // node features of the batch, goal-conditioned
       const double tm0 = elapsed_ms();
-      std::vector<uint32_t> cn(Q), cp(Q);
-      for (int i = 0; i < Q; i++) {
-        cn[i] = (uint32_t)cands[i].batch_node;
-        cp[i] = (uint32_t)cands[i].prim;
-      }
-      if (!b64.reserve((size_t)B * nx) || !feat.reserve((size_t)B * kMlpNodeFeat) || !pnode.reserve(Q) ||
-          !pprim.reserve(Q) || !mlp_out.reserve((size_t)Q * 2))
-        return DPG_ERR_OOM;
+      if (!b64.reserve((size_t)B * nx) || !feat.reserve((size_t)B * kMlpNodeFeat)) return DPG_ERR_OOM;
       cudaMemcpy(b64.p, bx.data(), sizeof(double) * bx.size(), cudaMemcpyHostToDevice);
-      cudaMemcpy(pnode.p, cn.data(), sizeof(uint32_t) * Q, cudaMemcpyHostToDevice);
-      cudaMemcpy(pprim.p, cp.data(), sizeof(uint32_t) * Q, cudaMemcpyHostToDevice);
       if ((rc = dpg_mlp_node_features(c, b64.p, B, goal, feat.p))) return rc;
-      if ((rc = dpg_mlp_forward(mlp, feat.p, pnode.p, pprim.p, Q, mlp_out.p))) return rc;
-      pred.resize((size_t)Q * 2);
-      cudaMemcpy(pred.data(), mlp_out.p, sizeof(float) * Q * 2, cudaMemcpyDeviceToHost);
       res->mlp_ms += elapsed_ms() - tm0;
     }
 
-    // insert or rewire, in pop order and the candidates' order (dbastar.cpp:809-919)
-    std::vector<int> accepted_as(Q, -1);  // node id of an accepted candidate
-    for (int b = 0; b < B; b++) {
-      const int parent = batch[b];
-      int n_new = 0;
-      for (int ci = first_cand[b]; ci < first_cand[b + 1]; ci++) {
-        Cand &cd = cands[ci];
-        double h = (o->heuristic == DPG_HEU_BLIND) ? 0.0 : lower_bound_time(r, cd.x.data(), goal);
-        if (o->heuristic == DPG_HEU_MLP) h = std::max(h, kCtgScale * std::max(0.0, (double)pred[2 * (size_t)ci + 1]));
-        const double g = (double)nodes[parent].g + cd.cost +
-                         o->cost_delta_factor * lower_bound_time(r, &xs[(size_t)parent * nx], cd.x0.data());
-        std::vector<int> nbr;
-        for (int k = 0; k < std::min(ct[ci], K); k++) nbr.push_back(it[(size_t)ci * K + k]);
-        for (int k = 0; k < std::min(cs[ci], K); k++) {
-          const int other = is[(size_t)ci * K + k];
-          if (accepted_as[other] >= 0) nbr.push_back(accepted_as[other]);
-        }
-        std::sort(nbr.begin(), nbr.end());
-        if (nbr.empty() || cd.chosen != -1) {
-          const int id = add_node(cd.x.data());
-          Node &n = nodes[id];
-          n.g = (float)g;
-          n.h = (float)h;
-          n.f = n.g + n.h;
-          n.parent = parent;
-          n.motion = cd.prim;
-          n.inter = cd.chosen;
-          n.in_open = true;
-          open.push({n.f, n.g, id, n.version});
-          accepted_as[ci] = id;
-          n_new++;
-        } else {
-          for (int nb : nbr) {
-            Node &n = nodes[nb];
-            const double tentative = g + lower_bound_time(r, cd.x.data(), &xs[(size_t)nb * nx]);
-            if (tentative < n.g) {
-              n.g = (float)tentative;
-              n.f = n.g + n.h;
-              n.parent = parent;
-              n.motion = cd.prim;
-              n.inter = -1;
-              n.version++;
-              n.in_open = true;
-              open.push({n.f, n.g, nb, n.version});
+    // Rounds of (prepare, query, insert/rewire): in each round every
+    // unfinished node, in pop order, visits its next chunk of motions (2 x the
+    // limit, doubling per round) until it has `limit` new nodes.  With one
+    // node per batch this is the reference's visiting order.
+    const int limit = o->limit_branching_factor;
+    std::vector<size_t> pos(B, 0), chunk(B, (size_t)2 * limit);
+    std::vector<int> n_new(B, 0);
+    std::vector<char> finished(B, 0);
+    for (int b = 0; b < B; b++) finished[b] = per_node[b].empty();
+    std::vector<int> first(B + 1, 0), c_node, c_prim, c_chosen, nbr;
+    std::vector<double> c_x, c_x0, c_cost;
+    while (std::find(finished.begin(), finished.end(), 0) != finished.end()) {
+      // successors of the round: end state (or the state meeting the goal),
+      // transformed motion start, cost
+      c_node.clear(); c_prim.clear(); c_chosen.clear(); c_x.clear(); c_x0.clear(); c_cost.clear();
+      for (int b = 0; b < B; b++) {
+        first[b] = (int)c_prim.size();
+        if (finished[b]) continue;
+        const double *x = &bx[(size_t)b * nx];
+        const size_t e = std::min(per_node[b].size(), pos[b] + chunk[b]);
+        for (size_t j = pos[b]; j < e; j++) {
+          const int p = per_node[b][j];
+          const int L = c->h_len[p];
+          const size_t q = c_prim.size();
+          c_node.push_back(b);
+          c_prim.push_back(p);
+          c_x.resize((q + 1) * nx);
+          c_x0.resize((q + 1) * nx);
+          transformed_state(r, st, c->h_soff[p], L - 1, x, &c_x[q * nx]);
+          transformed_state(r, st, c->h_soff[p], 0, x, &c_x0[q * nx]);
+          // check_goal: states at floor((k+1)/(n+1) * L), k = 0..3 (dbastar.cpp:492-512)
+          int chosen = -1;
+          double xi[16];
+          for (int k = 0; k < 4; k++) {
+            const int idx = (int)((float)(k + 1) / 5.0f * (float)L);
+            if (idx >= L) continue;
+            transformed_state(r, st, c->h_soff[p], idx, x, xi);
+            if (distance(r, xi, goal) <= goal_tol) {
+              std::memcpy(&c_x[q * nx], xi, sizeof(double) * nx);
+              chosen = idx;
+              break;
             }
           }
+          c_chosen.push_back(chosen);
+          c_cost.push_back((chosen != -1 ? chosen : L - 1) * r.dt);
         }
-        if (n_new >= o->limit_branching_factor) break;
+      }
+      first[B] = (int)c_prim.size();
+      const int Q = (int)c_prim.size();
+      if (Q == 0) break;
+
+      // novelty: successors vs explored nodes, and vs earlier successors of
+      // the round; the id capacity grows until every list is complete
+      const double tn0 = elapsed_ms();
+      if (!sync_table() || !q64.reserve((size_t)Q * nx) || !q32.reserve((size_t)Q * nx) || !cnt_tab.reserve(Q) ||
+          !cnt_self.reserve(Q))
+        return DPG_ERR_OOM;
+      std::vector<float> qf(c_x.begin(), c_x.end());
+      cudaMemcpy(q64.p, c_x.data(), sizeof(double) * c_x.size(), cudaMemcpyHostToDevice);
+      cudaMemcpy(q32.p, qf.data(), sizeof(float) * qf.size(), cudaMemcpyHostToDevice);
+      const int T = (int)nodes.size();
+      std::vector<int> ct(Q), cs(Q), it, is;
+      for (;;) {
+        if (!ids_tab.reserve((size_t)Q * Kq) || !ids_self.reserve((size_t)Q * Kq)) return DPG_ERR_OOM;
+        cudaMemset(cnt_tab.p, 0, sizeof(int) * Q);
+        cudaMemset(cnt_self.p, 0, sizeof(int) * Q);
+        with_kind_s(r.kind, [&](auto Kd) {
+          constexpr int KIND = decltype(Kd)::value;
+          for (int q0 = 0; q0 < Q; q0 += 65535) {  // grid.y limit
+            const int nq = std::min(65535, Q - q0);
+            dim3 g1((unsigned)std::min(64, (T + 255) / 256), (unsigned)nq);
+            radius_query<KIND><<<g1, 256>>>(c->rp, w32, q64.p, q32.p, Q, q0, t64.p, t32.p, T, nov_radius, 1e-5f, 0,
+                                            Kq, cnt_tab.p, ids_tab.p);
+            dim3 g2((unsigned)std::min(64, (Q + 255) / 256), (unsigned)nq);
+            radius_query<KIND><<<g2, 256>>>(c->rp, w32, q64.p, q32.p, Q, q0, q64.p, q32.p, Q, nov_radius, 1e-5f, 1,
+                                            Kq, cnt_self.p, ids_self.p);
+          }
+        });
+        cudaMemcpy(ct.data(), cnt_tab.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
+        if (cudaMemcpy(cs.data(), cnt_self.p, sizeof(int) * Q, cudaMemcpyDeviceToHost) != cudaSuccess)
+          return DPG_ERR_CUDA;
+        const int maxc = std::max(*std::max_element(ct.begin(), ct.end()), *std::max_element(cs.begin(), cs.end()));
+        if (maxc <= Kq) break;
+        Kq = maxc;
+      }
+      it.resize((size_t)Q * Kq);
+      is.resize((size_t)Q * Kq);
+      cudaMemcpy(it.data(), ids_tab.p, sizeof(int) * it.size(), cudaMemcpyDeviceToHost);
+      if (cudaMemcpy(is.data(), ids_self.p, sizeof(int) * is.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return DPG_ERR_CUDA;
+      res->novelty_ms += elapsed_ms() - tn0;
+
+      // learned heuristic: the surrogate's cost-to-go of every (node, motion)
+      // successor, never below the time lower bound
+      std::vector<float> pred;
+      if (o->heuristic == DPG_HEU_MLP) {
+        const double tm0 = elapsed_ms();
+        if (!pnode.reserve(Q) || !pprim.reserve(Q) || !mlp_out.reserve((size_t)Q * 2)) return DPG_ERR_OOM;
+        cudaMemcpy(pnode.p, c_node.data(), sizeof(uint32_t) * Q, cudaMemcpyHostToDevice);
+        cudaMemcpy(pprim.p, c_prim.data(), sizeof(uint32_t) * Q, cudaMemcpyHostToDevice);
+        if ((rc = dpg_mlp_forward(mlp, feat.p, pnode.p, pprim.p, Q, mlp_out.p))) return rc;
+        pred.resize((size_t)Q * 2);
+        cudaMemcpy(pred.data(), mlp_out.p, sizeof(float) * Q * 2, cudaMemcpyDeviceToHost);
+        res->mlp_ms += elapsed_ms() - tm0;
+      }
+
+      // insert or rewire, in pop order and the motions' order (dbastar.cpp:809-919)
+      std::vector<int> accepted_as(Q, -1);  // node id of an accepted successor
+      for (int b = 0; b < B; b++) {
+        if (finished[b]) continue;
+        const int parent = batch[b];
+        for (int ci = first[b]; ci < first[b + 1]; ci++) {
+          pos[b]++;
+          const double *cx = &c_x[(size_t)ci * nx];
+          double h = (o->heuristic == DPG_HEU_BLIND) ? 0.0 : lower_bound_time(r, cx, goal);
+          if (o->heuristic == DPG_HEU_MLP) h = std::max(h, kCtgScale * std::max(0.0, (double)pred[2 * (size_t)ci + 1]));
+          const double g = (double)nodes[parent].g + c_cost[ci] +
+                           o->cost_delta_factor * lower_bound_time(r, &xs[(size_t)parent * nx], &c_x0[(size_t)ci * nx]);
+          nbr.assign(it.begin() + (size_t)ci * Kq, it.begin() + (size_t)ci * Kq + ct[ci]);
+          for (int k = 0; k < cs[ci]; k++) {
+            const int other = is[(size_t)ci * Kq + k];
+            if (accepted_as[other] >= 0) nbr.push_back(accepted_as[other]);
+          }
+          std::sort(nbr.begin(), nbr.end());
+          if (nbr.empty() || c_chosen[ci] != -1) {
+            const int id = add_node(cx);
+            Node &n = nodes[id];
+            n.g = (float)g;
+            n.h = (float)h;
+            n.f = n.g + n.h;
+            n.parent = parent;
+            n.motion = c_prim[ci];
+            n.inter = c_chosen[ci];
+            n.in_open = true;
+            open.push({n.f, n.g, id, n.version});
+            accepted_as[ci] = id;
+            n_new[b]++;
+          } else {
+            for (int nb : nbr) {
+              Node &n = nodes[nb];
+              const double tentative = g + lower_bound_time(r, cx, &xs[(size_t)nb * nx]);
+              if (tentative < n.g) {
+                n.g = (float)tentative;
+                n.f = n.g + n.h;
+                n.parent = parent;
+                n.motion = c_prim[ci];
+                n.inter = -1;
+                n.version++;
+                n.in_open = true;
+                open.push({n.f, n.g, nb, n.version});
+              }
+            }
+          }
+          if (n_new[b] >= limit) break;
+        }
+        if (n_new[b] >= limit || pos[b] >= per_node[b].size()) finished[b] = 1;
+        else chunk[b] *= 2;  // chunk used up below the limit: a larger one next round
       }
     }
   }

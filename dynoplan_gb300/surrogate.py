@@ -26,6 +26,15 @@ def _p(t):
     return C.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def _ready(t):
+    """The library's streams are ordered after the legacy default stream
+    only: inputs produced on another torch stream are waited for here."""
+    import torch
+    s = torch.cuda.current_stream(t.device)
+    if s != torch.cuda.default_stream(t.device):
+        s.synchronize()
+
+
 class Surrogate:
     def __init__(self, n_prims: int, max_rows: int = 65536, device: int = 0, seed: int = 0):
         self.lib = _lib.load()
@@ -66,11 +75,13 @@ class Surrogate:
         n = node.numel()
         if out is None:
             out = torch.empty((n, 2), dtype=torch.float32, device=node.device)
+        _ready(node)
         check(self.lib.dpg_mlp_forward(self.h, _p(node_feat), _p(node), _p(prim), n, _p(out)))
         return out
 
     def train_step(self, node_feat, node, prim, target, lr=1e-3, ctg_weight=1.0) -> float:
         loss = C.c_float()
+        _ready(node)
         check(self.lib.dpg_mlp_train_step(self.h, _p(node_feat), _p(node), _p(prim), _p(target), node.numel(),
                                           lr, ctg_weight, C.byref(loss)))
         return loss.value
@@ -88,6 +99,7 @@ def node_features(ctx, x_dev, goal=None):
     N = x_dev.shape[0]
     feat = torch.empty((N, NODE_FEAT), dtype=torch.bfloat16, device=x_dev.device)
     g = None if goal is None else np.ascontiguousarray(goal, dtype=np.float64)
+    _ready(x_dev)
     check(_lib.load().dpg_mlp_node_features(ctx.h, _p(x_dev), N, g.ctypes.data if g is not None else None,
                                             _p(feat)), ctx.h)
     return feat
@@ -150,52 +162,68 @@ def make_dataset(wl, n_envs: int, nodes_per_env: int, pairs_per_env: int, seed: 
                    torch.from_numpy(np.concatenate(targets)).to(dev), n_envs, np.concatenate(env_of))
 
 
-def search_dataset(robot, prims, problems, opts, nodes_per_env: int = 600, radius: float | None = None,
-                   device: int = 0, log=None):
-    """Labels from completed searches and the exact checker, goal-conditioned:
-      - every (node, motion) pair on a solution path of a plain search, with
-        the remaining cost from its successor to the goal as cost-to-go and
+def search_dataset(robot, prims, problems, opts, nodes_per_env: int = 400, pairs_per_env: int = 20000,
+                   ctg_fraction: float = 0.3, radius: float | None = None, device: int = 0, seed: int = 0, log=None):
+    """Goal-conditioned labels from completed searches and the exact checker.
+      - cost-to-go: for the path s_0..s_n (motions m_1..m_n, durations
+        c_1..c_n) of every solved plain search and every i < j <= n, node s_i
+        with goal s_j (s_n: the problem's goal) and motion m_{i+1} is
+        labelled c_{i+2} + ... + c_j, the time left after the motion, and
         collision 0;
-      - every in-ball pair of `nodes_per_env` free nodes, exact-checked, with
-        its collision label (no cost-to-go: NaN).
+      - collision: `pairs_per_env` of the in-ball pairs of `nodes_per_env`
+        free nodes, exact-checked, with the problem's goal (cost-to-go NaN).
+    Cost-to-go rows are repeated to make about `ctg_fraction` of the rows.
     problems: list of (env, start, goal).  Returns (Dataset, search results)."""
     import torch
 
     from . import gpu as G
     from . import search as S
     radius = radius if radius is not None else opts.alpha * opts.delta
-    feats, nodes_g, prims_l, targets, results = [], [], [], [], []
-    base = 0
     dev = f"cuda:{device}"
+    rng = np.random.default_rng(seed)
+    feats, results = [], []
+    ctg_rows, coll_rows = [], []   # (node row, prim, collision, ctg)
+    base = 0
+
+    def add_feats(x, goal):
+        nonlocal base
+        x_dev = torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to(dev)
+        feats.append(node_features(ctx, x_dev, goal))
+        base += len(x)
+        return base - len(x)
+
     with G.Context(robot, device=device) as ctx:
         ctx.upload_primitives(prims)
         for i, (env, start, goal) in enumerate(problems):
             ctx.upload_env(env)
             res, motions, states = S.search(ctx, start, goal, opts)
             results.append(res)
-            rand = W.make_nodes(robot, env, nodes_per_env, seed=7000 + i, vel_sigma=0.5)
-            node_states = np.concatenate([states[:-1], rand], 0) if res["solved"] else rand
-            x_dev = torch.from_numpy(np.ascontiguousarray(node_states)).to(dev)
-            feats.append(node_features(ctx, x_dev, goal))
-            n_path = len(motions) if res["solved"] else 0
-            if n_path:
+            n = len(motions) if res["solved"] else 0
+            if n:
                 cost = np.array([(int(prims.length[p]) - 1) * robot.dt for p in motions])
-                remaining = cost[::-1].cumsum()[::-1] - cost   # after motion i
-                nodes_g.append(np.arange(n_path) + base)
-                prims_l.append(motions.astype(np.int64))
-                targets.append(np.stack([np.zeros(n_path), remaining / CTG_SCALE], 1).astype(np.float32))
+                cost[-1] = res["cost"] - cost[:-1].sum()
+                for j in range(1, n + 1):
+                    r0 = add_feats(states[:j], goal if j == n else states[j])
+                    left = np.array([cost[i + 1:j].sum() for i in range(j)])
+                    ctg_rows.append(np.stack([r0 + np.arange(j), motions[:j], np.zeros(j), left / CTG_SCALE], 1))
+            rand = W.make_nodes(robot, env, nodes_per_env, seed=7000 + 31 * i + seed, vel_sigma=0.5)
+            r0 = add_feats(rand, goal)
             exp = ctx.expand(rand, radius, precision=0)
-            nodes_g.append(exp["node"].astype(np.int64) + n_path + base)
-            prims_l.append(exp["prim"].astype(np.int64))
-            targets.append(np.stack([(exp["verdict"] != 0).astype(np.float32),
-                                     np.full(exp["n_pairs"], np.nan, np.float32)], 1))
-            base += len(node_states)
+            keep = rng.choice(exp["n_pairs"], size=min(pairs_per_env, exp["n_pairs"]), replace=False)
+            coll_rows.append(np.stack([r0 + exp["node"][keep].astype(np.float64), exp["prim"][keep],
+                                       (exp["verdict"][keep] != 0), np.full(len(keep), np.nan)], 1))
             if log:
                 log(f"problem {i}: {res['status_str']} cost {res['cost']:.2f} in {res['time_ms']:.0f} ms")
+    coll = np.concatenate(coll_rows) if coll_rows else np.zeros((0, 4))
+    ctg = np.concatenate(ctg_rows) if ctg_rows else np.zeros((0, 4))
+    if len(ctg):
+        reps = max(1, int(round(ctg_fraction / (1 - ctg_fraction) * len(coll) / len(ctg))))
+        ctg = np.repeat(ctg, reps, axis=0)
+    rows = np.concatenate([ctg, coll])
     ds = Dataset(torch.cat(feats, 0).contiguous(),
-                 torch.from_numpy(np.concatenate(nodes_g).astype(np.int32)).to(dev),
-                 torch.from_numpy(np.concatenate(prims_l).astype(np.int32)).to(dev),
-                 torch.from_numpy(np.concatenate(targets)).to(dev), len(problems), None)
+                 torch.from_numpy(rows[:, 0].astype(np.int32)).to(dev),
+                 torch.from_numpy(rows[:, 1].astype(np.int32)).to(dev),
+                 torch.from_numpy(rows[:, 2:4].astype(np.float32)).to(dev), len(problems), None)
     return ds, results
 
 

@@ -21,7 +21,11 @@
  *     dpg_last_error() gives the context's last message.
  *   - A context belongs to one host thread at a time (the reference Expander
  *     holds mutable scratch too, dbastar.hpp:233-313).  All device work of a
- *     context runs on its own CUDA stream.
+ *     context runs on its own blocking CUDA stream, so it is ordered after
+ *     work already queued on the legacy default stream; device-resident
+ *     inputs written on any other stream must be complete (synchronise that
+ *     stream) before the call.  Every call has finished its device work
+ *     when it returns.
  *   - Input arrays are copied; the caller keeps ownership.  Output arrays
  *     are owned by the caller (host or device memory, see dpg_expand_opts).
  *   - Precision: DPG_FP32 computes rollouts and separating-axis tests in

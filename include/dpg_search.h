@@ -12,10 +12,14 @@
  * float scores (compareAStarNode, dbastar.cpp:56-68).
  *
  * GPU form: `batch` open nodes are popped per iteration and expanded in one
- * dpg_expand call; the novelty queries of all their candidate successors run
- * as one brute-force radius query on the GPU (FP32 with an FP64 re-test near
- * the radius); insertion and rewiring then follow the reference's order on
- * the host.  batch = 1 visits nodes in the reference's order.
+ * dpg_expand call.  The reference visits a node's motions in order and stops
+ * at the limit, so successors are prepared in rounds: each unfinished node,
+ * in pop order, visits its next chunk of valid motions (2 x the limit,
+ * doubling per round) until it has `limit` new nodes.  The novelty queries
+ * of a round run as one brute-force radius query on the GPU (FP32 with an
+ * FP64 re-test near the radius; neighbour lists are complete, whatever
+ * their length); insertion and rewiring run on the host in that order.
+ * batch = 1 visits nodes and motions in the reference's order.
  */
 #ifndef DPG_SEARCH_H
 #define DPG_SEARCH_H
@@ -54,7 +58,8 @@ typedef struct dpg_search_opts {
   int32_t shuffle;                /* 1: shuffle each node's candidates (std::mt19937 seeded
                                      with `seed`, then std::shuffle, as expand_lazy);
                                      0: ascending motion index */
-  int32_t max_neighbors;          /* explored nodes considered for rewiring per successor */
+  int32_t max_neighbors;          /* initial neighbour-list capacity per successor (it grows
+                                     to the largest neighbour count; lists are complete) */
   uint64_t seed;
 } dpg_search_opts;
 

@@ -127,43 +127,44 @@ def search(m, prims, env, start, goal, delta, alpha=0.5, batch=1, limit=20, max_
                         break
                 cost = (chosen if chosen != -1 else L - 1) * m.dt
                 cands.append((b, int(p), xe, x0, chosen, cost))
-        n_before = len(X)
-        Xn = np.array(X)
-        accepted = {}
-        for b, parent_i in enumerate(bat):
-            n_new = 0
-            for ci, (cb, p, xe, x0, chosen, cost) in enumerate(cands):
-                if cb != b:
+        # rounds: every unfinished node, in pop order, visits its next chunk
+        # of motions (2 x limit, doubling) until it has `limit` new nodes
+        per = [[c for c in cands if c[0] == b] for b in range(len(bat))]
+        pos, chunk, n_new = [0] * len(bat), [2 * limit] * len(bat), [0] * len(bat)
+        finished = [len(per[b]) == 0 for b in range(len(bat))]
+        while not all(finished):
+            for b, parent_i in enumerate(bat):
+                if finished[b]:
                     continue
-                hh = f32(lbt(m, xe, goal)) if heuristic == 0 else f32(0)
-                gg = float(g[parent_i]) + cost + cdf * float(lbt(m, X[parent_i], x0))
-                d_tab = distance(m, Xn, xe[None, :]) if n_before else np.zeros(0)
-                nbr = list(np.flatnonzero(d_tab <= nov))
-                for cj, nid in accepted.items():
-                    if cj < ci and distance(m, cands[cj][2], xe) <= nov:
-                        nbr.append(nid)
-                nbr = sorted(nbr)
-                if not nbr or chosen != -1:
-                    X.append(xe)
-                    nid = len(X) - 1
-                    g.append(f32(gg)); h.append(hh); f.append(f32(f32(gg) + hh))
-                    parent.append(parent_i); motion.append(p); inter.append(chosen); version.append(0)
-                    in_open.append(True)
-                    heapq.heappush(heap, (f[nid], -g[nid], nid, 0))
-                    accepted[ci] = nid
-                    n_new += 1
+                for (cb, p, xe, x0, chosen, cost) in per[b][pos[b]:pos[b] + chunk[b]]:
+                    pos[b] += 1
+                    hh = f32(lbt(m, xe, goal)) if heuristic == 0 else f32(0)
+                    gg = float(g[parent_i]) + cost + cdf * float(lbt(m, X[parent_i], x0))
+                    nbr = sorted(np.flatnonzero(distance(m, np.array(X), xe[None, :]) <= nov))
+                    if not nbr or chosen != -1:
+                        X.append(xe)
+                        nid = len(X) - 1
+                        g.append(f32(gg)); h.append(hh); f.append(f32(f32(gg) + hh))
+                        parent.append(parent_i); motion.append(p); inter.append(chosen); version.append(0)
+                        in_open.append(True)
+                        heapq.heappush(heap, (f[nid], -g[nid], nid, 0))
+                        n_new[b] += 1
+                    else:
+                        for nb in nbr:
+                            tent = gg + float(lbt(m, xe, X[nb]))
+                            if tent < g[nb]:
+                                g[nb] = f32(tent)
+                                f[nb] = f32(g[nb] + h[nb])
+                                parent[nb], motion[nb], inter[nb] = parent_i, p, -1
+                                version[nb] += 1
+                                in_open[nb] = True
+                                heapq.heappush(heap, (f[nb], -g[nb], nb, version[nb]))
+                    if n_new[b] >= limit:
+                        break
+                if n_new[b] >= limit or pos[b] >= len(per[b]):
+                    finished[b] = True
                 else:
-                    for nb in nbr:
-                        tent = gg + float(lbt(m, xe, X[nb]))
-                        if tent < g[nb]:
-                            g[nb] = f32(tent)
-                            f[nb] = f32(g[nb] + h[nb])
-                            parent[nb], motion[nb], inter[nb] = parent_i, p, -1
-                            version[nb] += 1
-                            in_open[nb] = True
-                            heapq.heappush(heap, (f[nb], -g[nb], nb, version[nb]))
-                if n_new >= limit:
-                    break
+                    chunk[b] *= 2
     out = {"solved": solution >= 0, "status": status, "expands": expands, "nodes": len(X)}
     if solution >= 0:
         chain = []
