@@ -64,6 +64,13 @@ def parse():
     return ap.parse_args()
 
 
+def _np_json(o):
+    """numpy scalars in the JSON line"""
+    if hasattr(o, "item"):
+        return o.item()
+    raise TypeError(type(o).__name__)
+
+
 def dist_info():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -280,7 +287,7 @@ def run_reference(args, rank, world):
         "note": "CPU restatement of the reference expand (oracle/oracle.c orc_expand_fast); the "
                 "reference's C++ does not build here (dynobench, nigh, fcl, OMPL absent)",
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_np_json), flush=True)
 
 
 def run_ours(args, rank, world, local_rank):
@@ -288,6 +295,7 @@ def run_ours(args, rank, world, local_rank):
 
     from dynoplan_gb300 import _lib
     from dynoplan_gb300 import gpu as G
+    from dynoplan_gb300 import replicas
     from dynoplan_gb300 import workloads as W
 
     lib = _lib.load()
@@ -346,14 +354,8 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
-    total_s = sum(dev_ms) * 1e-3
-    if world > 1:
-        tt = torch.tensor([total_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(tt.item())
-        pp = torch.tensor([pairs_total], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(pp)
-        pairs_total = int(pp.item())
+    total_s, pairs_total = replicas.reduce_step(sum(dev_ms) * 1e-3, pairs_total, device=dev)
+    pairs_total = int(pairs_total)
     value = pairs_total / total_s
 
     # work model of the exact check, from the last step's outputs
@@ -415,7 +417,7 @@ def run_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_np_json), flush=True)
 
 
 def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
@@ -579,7 +581,7 @@ def run_surrogate(args, rank, world, local_rank):
         "gpu_launches": MLP_KERNELS_PER_TRAIN_STEP * args.steps,
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_np_json), flush=True)
 
 
 # --------------------------------------------- end-to-end search (quad2d) --
@@ -656,7 +658,7 @@ def run_search(args, rank, world, local_rank):
         "median_cost_ratio_mlp": statistics.median(cost_ratio) if cost_ratio else None,
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_np_json), flush=True)
 
 
 def ctypes_peak(lib, dev):

@@ -109,6 +109,31 @@ template <class F> void with_kind(int kind, F &&f) {
 
 }  // namespace
 
+// The exact check of the pair list on `st`: lockstep warps over (primitive,
+// 32 nodes) items, with obstacle culling when the candidate masks cover
+// every obstacle.
+template <int KIND>
+static void launch_check(dpg_ctx *c, const CheckArgs &ca, bool fp64, cudaStream_t st) {
+  using R = Robot<KIND>;
+  const bool cull = c->n_obs <= kMaxCullObs;
+  const size_t ob = fp64 ? (R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>))
+                         : (R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>));
+  const size_t sm = ob * std::max(c->n_obs, 1);
+  auto go = [&](auto kern) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
+    kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+  };
+  if (fp64) {
+    if (cull) go(check_pairs<KIND, double, false, true>);
+    else go(check_pairs<KIND, double, false, false>);
+  } else {
+    if (cull) go(check_pairs<KIND, float, true, true>);
+    else go(check_pairs<KIND, float, true, false>);
+  }
+}
+
 // primitive tiles per nn_mask block: small node batches are split over the
 // primitives too, for about two blocks per SM
 static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
@@ -497,7 +522,6 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   ca.radius32 = (float)rp.radius;
   ca.band32 = (float)ca.band;
   for (int i = 0; i < 3; i++) { ca.lo32[i] = (float)c->lo[i]; ca.hi32[i] = (float)c->hi[i]; }
-  const bool cull = c->n_obs <= kMaxCullObs;
 
   cudaError_t launch_err = cudaSuccess;
   with_kind(kind, [&](auto K) {
@@ -524,24 +548,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     }
     cudaEventRecord(c->ev[2], st);
     // exact check: persistent grid, obstacles in shared memory
-    const size_t obs_bytes32 = R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>);
-    const size_t obs_bytes64 = R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>);
-    auto launch = [&](auto kern, size_t obs_bytes) {
-      const size_t sm = obs_bytes * std::max(c->n_obs, 1);
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      int per_sm = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
-      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
-    };
-    if (opts->mode & DPG_MODE_BALL_ONLY) {
-      // pairs only: no exact check
-    } else if (fp64) {
-      if (cull) launch(check_pairs<KIND, double, false, true>, obs_bytes64);
-      else launch(check_pairs<KIND, double, false, false>, obs_bytes64);
-    } else {
-      if (cull) launch(check_pairs<KIND, float, true, true>, obs_bytes32);
-      else launch(check_pairs<KIND, float, true, false>, obs_bytes32);
-    }
+    if (!(opts->mode & DPG_MODE_BALL_ONLY)) launch_check<KIND>(c, ca, fp64, st);  // ball-only: pairs, no check
     cudaEventRecord(c->ev[3], st);
     cudaEventRecord(c->ev[4], st);
     launch_err = cudaGetLastError();
@@ -738,7 +745,6 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
   ca.radius32 = (float)rp.radius;
   ca.band32 = (float)ca.band;
   for (int i = 0; i < 3; i++) { ca.lo32[i] = (float)c->lo[i]; ca.hi32[i] = (float)c->hi[i]; }
-  const bool cull = c->n_obs <= kMaxCullObs;
 
   cudaError_t launch_err = cudaSuccess;
   with_kind(kind, [&](auto K) {
@@ -760,22 +766,7 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
       dim3 eg((unsigned)((Ppad / 32 + 7) / 8), (unsigned)B);
       nn_emit<<<eg, 256, 0, st>>>(P, Ppad, W, mask, cnt, pbase, cap, po.node, po.prim);
     }
-    const size_t obs_bytes32 = R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>);
-    const size_t obs_bytes64 = R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>);
-    auto launch = [&](auto kern, size_t obs_bytes) {
-      const size_t sm = obs_bytes * std::max(c->n_obs, 1);
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      int per_sm = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
-      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
-    };
-    if (fp64) {
-      if (cull) launch(check_pairs<KIND, double, false, true>, obs_bytes64);
-      else launch(check_pairs<KIND, double, false, false>, obs_bytes64);
-    } else {
-      if (cull) launch(check_pairs<KIND, float, true, true>, obs_bytes32);
-      else launch(check_pairs<KIND, float, true, false>, obs_bytes32);
-    }
+    launch_check<KIND>(c, ca, fp64, st);
     launch_err = cudaGetLastError();
   });
   if (launch_err != cudaSuccess)
@@ -941,7 +932,6 @@ extern "C" int dpg_check_pairs(dpg_ctx *c, const dpg_expand_opts *opts, int64_t 
   ca.radius32 = (float)rp.radius;
   ca.band32 = (float)ca.band;
   for (int i = 0; i < 3; i++) { ca.lo32[i] = (float)c->lo[i]; ca.hi32[i] = (float)c->hi[i]; }
-  const bool cull = c->n_obs <= kMaxCullObs;
 
   CUDA_TRY(c, cudaEventRecord(c->ev[1], st));
   CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), st));
@@ -960,22 +950,7 @@ extern "C" int dpg_check_pairs(dpg_ctx *c, const dpg_expand_opts *opts, int64_t 
                                                                P_<uint32_t>(c->q_fill), P_<uint32_t>(c->q_sorted),
                                                                P_<uint32_t>(c->q_idx));
     cudaEventRecord(c->ev[2], st);
-    const size_t obs_bytes = fp64 ? (R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>))
-                                  : (R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>));
-    auto launch = [&](auto kern) {
-      const size_t sm = obs_bytes * std::max(c->n_obs, 1);
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      int per_sm = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
-      kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
-    };
-    if (fp64) {
-      if (cull) launch(check_pairs<KIND, double, false, true>);
-      else launch(check_pairs<KIND, double, false, false>);
-    } else {
-      if (cull) launch(check_pairs<KIND, float, true, true>);
-      else launch(check_pairs<KIND, float, true, false>);
-    }
+    launch_check<KIND>(c, ca, fp64, st);
     cudaEventRecord(c->ev[3], st);
     launch_err = cudaGetLastError();
   });
