@@ -14,6 +14,7 @@
 // thread (tcgen05.ld 32x32b) and hands 16 columns at a time to `Epi`.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "umma.cuh"
@@ -104,6 +105,125 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_bf16_tn(const __nv_bfloat16
     if (threadIdx.x == 0) atomicExch(err, 1);
     // let in-flight MMAs finish before the tensor memory is released
     if (issued > 0) umma::mbar_wait(&mbar[(issued - 1) & 1], ((issued - 1) >> 1) & 1, 1u << 20);
+  } else if (nchunks > 0) {
+    umma::fence_after_sync();
+    const int row = 32 * warp + lane;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      float v[16];
+      umma::tmem_ld16(lane_addr + c0, v);
+      if (m0 + row < M) epi(m0 + row, c0, v);
+    }
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, kCols);
+}
+
+// ---- TMA-fed, warp-specialised form ------------------------------------------
+//
+// Same contract and tile (128 rows x all N columns in TMEM, K in 64-wide
+// SW128 k-blocks), but the operands arrive by TMA (cp.async.bulk.tensor,
+// 128-byte swizzle written by the copy engine) into a ring of S stages:
+// thread 0 of warp 0 issues the loads, thread 0 of warp 1 the MMAs; a stage
+// is refilled once the MMAs that read it have committed to its `empty`
+// barrier.  All four warps run the epilogue.  Rows beyond M load as zeros.
+// Every wait is bounded; on expiry the kernel sets *err, waits (bounded)
+// for its copies and MMAs in flight, frees its tensor memory and returns.
+__host__ __device__ constexpr int tma_stages(int N) {
+  return (110 * 1024) / (128 * 128 + N * 128) < 2 ? 2
+         : ((110 * 1024) / (128 * 128 + N * 128) > 4 ? 4 : (110 * 1024) / (128 * 128 + N * 128));
+}
+__host__ __device__ constexpr size_t gemm_tma_smem_bytes(int N) {
+  return (size_t)tma_stages(N) * (128 * 128 + N * 128) + 1024 + 256;
+}
+
+template <int N, class Epi>
+__global__ void __launch_bounds__(kGemmThreads) gemm_bf16_tma(const __grid_constant__ CUtensorMap tmA,
+                                                               const __grid_constant__ CUtensorMap tmB, int M,
+                                                               int K, int k_per_split, Epi epi, int *err) {
+  static_assert(N % 16 == 0 && N >= 16 && N <= 256, "N");
+  constexpr int S = tma_stages(N);
+  constexpr uint32_t kA = 128 * 128, kB = N * 128, kStage = kA + kB;
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = umma::smem_u32(smem_raw);
+  unsigned char *base = smem_raw + ((1024 - (raw & 1023)) & 1023);
+  uint64_t *full = reinterpret_cast<uint64_t *>(base + S * kStage);
+  uint64_t *empty = full + S;
+  uint64_t *done = empty + S;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+  __shared__ int s_bad;
+
+  const int m0 = blockIdx.x * 128;
+  const int kbeg = blockIdx.y * k_per_split;
+  const int kend = min(K, kbeg + k_per_split);
+  const int nchunks = (kend - kbeg) / kGemmKChunk;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr uint32_t kCols = tmem_cols_for(N);
+  constexpr uint32_t idesc = umma::idesc_bf16_f32(128, N);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; s++) {
+      umma::mbar_init(&full[s], 1);
+      umma::mbar_init(&empty[s], 1);
+    }
+    umma::mbar_init(done, 1);
+    umma::mbar_fence_init();
+    s_bad = 0;
+  }
+  if (warp == 0) {
+    umma::tmem_alloc(tslot, kCols);
+    umma::tmem_relinquish();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+
+  int loads = 0;  // (thread 0) chunks whose loads were issued
+  if (threadIdx.x == 0) {
+    // producer
+    for (int i = 0; i < nchunks; i++) {
+      const int s = i % S;
+      if (i >= S && !umma::mbar_wait(&empty[s], ((i / S) - 1) & 1)) {
+        s_bad = 1;
+        break;
+      }
+      if (*(volatile int *)&s_bad) break;
+      unsigned char *a = base + s * kStage;
+      umma::mbar_arrive_expect_tx(&full[s], kStage);
+      umma::tma_load_2d(a, &tmA, kbeg + i * kGemmKChunk, m0, &full[s]);
+      umma::tma_load_2d(a + kA, &tmB, kbeg + i * kGemmKChunk, 0, &full[s]);
+      loads = i + 1;
+    }
+  } else if (threadIdx.x == 32) {
+    // MMA issuer
+    for (int i = 0; i < nchunks; i++) {
+      const int s = i % S;
+      if (!umma::mbar_wait(&full[s], (i / S) & 1)) {
+        s_bad = 1;
+        break;
+      }
+      umma::fence_after_sync();
+      const uint32_t a0 = umma::smem_u32(base + s * kStage), b0 = a0 + kA;
+#pragma unroll
+      for (int kk = 0; kk < kGemmKChunk / 16; kk++)
+        umma::mma_bf16(tmem, umma::sdesc_kmajor_sw128(a0 + kk * 32), umma::sdesc_kmajor_sw128(b0 + kk * 32),
+                       idesc, (i > 0 || kk > 0) ? 1u : 0u);
+      umma::commit(&empty[s]);
+    }
+    umma::commit(done);  // arrives once every MMA issued above is complete
+  }
+  // everyone: the accumulator is final once `done` completes
+  const bool ok = nchunks > 0 && umma::mbar_wait(done, 0);
+  const bool bad = __syncthreads_or(!ok || s_bad) && nchunks > 0;
+  if (bad) {
+    if (threadIdx.x == 0) {
+      atomicExch(err, 1);
+      // copies still in flight land before the block's shared memory goes
+      for (int i = max(0, loads - S); i < loads; i++) umma::mbar_wait(&full[i % S], (i / S) & 1, 1u << 20);
+    }
   } else if (nchunks > 0) {
     umma::fence_after_sync();
     const int row = 32 * warp + lane;

@@ -13,16 +13,57 @@ using namespace dpg;
 
 namespace {
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// tensor map of a row-major bf16 matrix [rows x k] read in boxes of
+// 64 columns (one 128-byte swizzle row) x box_rows rows
+bool make_kmajor_map(CUtensorMap *m, const void *ptr, uint64_t rows, uint64_t k, uint32_t box_rows) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn || (reinterpret_cast<uintptr_t>(ptr) & 15) || k % kGemmKChunk) return false;
+  const cuuint64_t dims[2] = {k, rows};
+  const cuuint64_t strides[1] = {k * sizeof(__nv_bfloat16)};
+  const cuuint32_t box[2] = {(cuuint32_t)kGemmKChunk, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool g_gemm_tma = true;  // surrogate GEMMs through the TMA-fed kernel
+
 template <int N, class Epi>
 cudaError_t launch_gemm_n(const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int K, int split, Epi epi,
-                          int *err, cudaStream_t st) {
+                          int *err, cudaStream_t st, bool tma) {
+  const int kchunks = K / kGemmKChunk;
+  const int per = (kchunks + split - 1) / split * kGemmKChunk;
+  dim3 grid((M + 127) / 128, (K + per - 1) / per);
+  CUtensorMap ta, tb;
+  if (tma && make_kmajor_map(&ta, A, (uint64_t)M, (uint64_t)K, 128) && make_kmajor_map(&tb, B, N, (uint64_t)K, N)) {
+    auto kern = gemm_bf16_tma<N, Epi>;
+    const size_t sm = gemm_tma_smem_bytes(N);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kGemmThreads, sm, st>>>(ta, tb, M, K, per, epi, err);
+    return cudaGetLastError();
+  }
   auto kern = gemm_bf16_tn<N, Epi>;
   const size_t sm = gemm_smem_bytes(N);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  const int kchunks = K / kGemmKChunk;
-  const int per = (kchunks + split - 1) / split * kGemmKChunk;
-  dim3 grid((M + 127) / 128, (K + per - 1) / per);
   kern<<<grid, kGemmThreads, sm, st>>>(A, B, M, K, per, epi, err);
   return cudaGetLastError();
 }
@@ -30,11 +71,11 @@ cudaError_t launch_gemm_n(const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M,
 // N (multiple of 16, <= 256) as a template argument
 template <class Epi>
 cudaError_t launch_gemm(int N, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int K, int split, Epi epi,
-                        int *err, cudaStream_t st) {
+                        int *err, cudaStream_t st, bool tma = g_gemm_tma) {
   switch (N) {
 #define DPG_GEMM_CASE(n) \
   case n:                \
-    return launch_gemm_n<n>(A, B, M, K, split, epi, err, st);
+    return launch_gemm_n<n>(A, B, M, K, split, epi, err, st, tma);
     DPG_GEMM_CASE(16) DPG_GEMM_CASE(32) DPG_GEMM_CASE(48) DPG_GEMM_CASE(64) DPG_GEMM_CASE(80)
     DPG_GEMM_CASE(96) DPG_GEMM_CASE(112) DPG_GEMM_CASE(128) DPG_GEMM_CASE(144) DPG_GEMM_CASE(160)
     DPG_GEMM_CASE(176) DPG_GEMM_CASE(192) DPG_GEMM_CASE(208) DPG_GEMM_CASE(224) DPG_GEMM_CASE(240)
@@ -58,15 +99,17 @@ extern "C" int dpg_gemm_bf16(const void *A_dev, const void *B_dev, float *C_dev,
     gemm_bf16_ref<<<(unsigned)((n + 255) / 256), 256>>>(A, B, C_dev, M, N, K);
     return cudaDeviceSynchronize() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
   }
-  if (impl != 0 || N % 16 || N > 256 || K % kGemmKChunk || split_k < 1) return DPG_ERR_ARG;
+  if ((impl != 0 && impl != 2) || N % 16 || N > 256 || K % kGemmKChunk || split_k < 1) return DPG_ERR_ARG;
+  const bool tma = impl == 2;
+  if (tma && !encode_tiled()) return DPG_ERR_NODEVICE;
   if (!g_err && cudaMalloc(&g_err, sizeof(int)) != cudaSuccess) return DPG_ERR_OOM;
   cudaMemset(g_err, 0, sizeof(int));
   cudaError_t e;
   if (split_k > 1) {
     cudaMemset(C_dev, 0, sizeof(float) * (size_t)M * N);
-    e = launch_gemm(N, A, B, M, K, split_k, EpiAtomicF32{C_dev, N, N}, g_err, 0);
+    e = launch_gemm(N, A, B, M, K, split_k, EpiAtomicF32{C_dev, N, N}, g_err, 0, tma);
   } else {
-    e = launch_gemm(N, A, B, M, K, 1, EpiStoreF32{C_dev, N, N}, g_err, 0);
+    e = launch_gemm(N, A, B, M, K, 1, EpiStoreF32{C_dev, N, N}, g_err, 0, tma);
   }
   if (e != cudaSuccess) return DPG_ERR_CUDA;
   if (cudaDeviceSynchronize() != cudaSuccess) return DPG_ERR_CUDA;

@@ -121,6 +121,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// ---- TMA ----------------------------------------------------------------------
+// The barrier expects `bytes` more transaction bytes and receives one arrive.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+// 2-D tiled bulk tensor load (box of the tensor map at element coordinates
+// x = innermost, y) into shared memory; completes transaction bytes on `bar`.
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *tmap, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // ---- operand staging -----------------------------------------------------------
 // byte offset of (row r, 16-byte chunk g) in a K-major SW128 tile of R rows
 __device__ __forceinline__ uint32_t kmajor_offset(int R, int r, int g) {

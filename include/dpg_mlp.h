@@ -24,8 +24,11 @@ extern "C" {
 #endif
 
 /* C[M x N] (FP32, row-major) = A[M x K] * B[N x K]^T with A, B bf16
- * row-major.  impl 0: tcgen05 tensor-core kernel (N a multiple of 16,
- * <= 256; K a multiple of 64); impl 1: CUDA-core reference.  split_k > 1
+ * row-major.  impl 0: tcgen05 tensor-core kernel with thread-staged
+ * operands (N a multiple of 16, <= 256; K a multiple of 64); impl 2: the
+ * same MMA fed by TMA through a multi-stage shared-memory ring (same shape
+ * rules; A and B 16-byte aligned; the surrogate's default); impl 1:
+ * CUDA-core reference.  split_k > 1
  * splits K over that many CTAs per row tile (C is zeroed first).  Runs on the
  * current device's default stream and waits. */
 int dpg_gemm_bf16(const void *A_dev, const void *B_dev, float *C_dev, int M, int N, int K, int impl,
