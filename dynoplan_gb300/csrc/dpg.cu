@@ -256,10 +256,12 @@ void dpg_destroy(dpg_ctx *c) {
 
 const char *dpg_last_error(const dpg_ctx *c) { return c ? c->err.c_str() : "null context"; }
 
-int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const double *states,
-                          const double *actions) {
-  if (!c) return DPG_ERR_ARG;
-  if (P <= 0 || !len || !states || !actions) return fail(c, DPG_ERR_ARG, "upload_primitives: empty input");
+}  // extern "C"
+
+// Host index, raw device tables and every derived table of a primitive set.
+// `states` / `actions` are host arrays (H2D) or device arrays (D2D, `kind`).
+static int load_tables(dpg_ctx *c, int32_t P, const int32_t *len, const double *states, const double *actions,
+                       cudaMemcpyKind copy) {
   const int nx = c->robot.nx, nu = c->robot.nu, kind = c->robot.kind;
   c->h_len.assign(len, len + P);
   c->h_soff.resize(P);
@@ -305,9 +307,8 @@ int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const doubl
   CUDA_TRY(c, cudaMemcpyAsync(c->aoff.p, c->h_aoff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->order.p, c->h_order.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->coff.p, c->h_coff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(c, cudaMemcpyAsync(c->st64.p, states, sizeof(double) * nx * S, cudaMemcpyHostToDevice, st));
-  if (A > 0)
-    CUDA_TRY(c, cudaMemcpyAsync(c->act64.p, actions, sizeof(double) * nu * A, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->st64.p, states, sizeof(double) * nx * S, copy, st));
+  if (A > 0) CUDA_TRY(c, cudaMemcpyAsync(c->act64.p, actions, sizeof(double) * nu * A, copy, st));
   const RobotParams rp = c->rp;
   with_kind(kind, [&](auto K) {
     constexpr int KIND = decltype(K)::value;
@@ -333,6 +334,62 @@ int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const doubl
   c->A = A;
   c->have_prims = true;
   return DPG_OK;
+}
+
+extern "C" {
+
+int dpg_upload_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const double *states,
+                          const double *actions) {
+  if (!c) return DPG_ERR_ARG;
+  if (P <= 0 || !len || !states || !actions) return fail(c, DPG_ERR_ARG, "upload_primitives: empty input");
+  return load_tables(c, P, len, states, actions, cudaMemcpyHostToDevice);
+}
+
+int dpg_prepend_primitives(dpg_ctx *c, int32_t P, const int32_t *len, const double *states,
+                           const double *actions) {
+  if (!c) return DPG_ERR_ARG;
+  if (P <= 0 || !len || !states || !actions) return fail(c, DPG_ERR_ARG, "prepend_primitives: empty input");
+  if (!c->have_prims) return load_tables(c, P, len, states, actions, cudaMemcpyHostToDevice);
+  const int nx = c->robot.nx, nu = c->robot.nu;
+  int64_t S = 0, A = 0;
+  for (int p = 0; p < P; p++) {
+    if (len[p] < 1 || len[p] > 32767) return fail(c, DPG_ERR_ARG, "prepend_primitives: length out of [1, 32767]");
+    S += len[p];
+    A += len[p] - 1;
+  }
+  // the combined raw tables, new motions first; the old ones stay on the device
+  // (for rollout robots their rows are the canonical rollout of the stored
+  // start and actions, which the derivation reproduces exactly)
+  std::vector<int32_t> all(len, len + P);
+  all.insert(all.end(), c->h_len.begin(), c->h_len.end());
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  DevBuf st{}, ac{};
+  int rc;
+  if ((rc = ensure(c, st, sizeof(double) * nx * (S + c->S))) ||
+      (rc = ensure(c, ac, sizeof(double) * nu * std::max<int64_t>(A + c->A, 1)))) {
+    release(st);
+    release(ac);
+    return rc;
+  }
+  cudaStream_t s = c->stream;
+  double *st_p = P_<double>(st), *ac_p = P_<double>(ac);
+  cudaError_t e = cudaMemcpyAsync(st_p, states, sizeof(double) * nx * S, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(st_p + nx * S, c->st64.p, sizeof(double) * nx * c->S, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && A > 0)
+    e = cudaMemcpyAsync(ac_p, actions, sizeof(double) * nu * A, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && c->A > 0)
+    e = cudaMemcpyAsync(ac_p + nu * A, c->act64.p, sizeof(double) * nu * c->A, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    release(st);
+    release(ac);
+    return fail(c, DPG_ERR_CUDA, std::string("prepend_primitives: ") + cudaGetErrorString(e));
+  }
+  rc = load_tables(c, (int32_t)all.size(), all.data(), st_p, ac_p, cudaMemcpyDeviceToDevice);
+  release(st);
+  release(ac);
+  return rc;
 }
 
 int dpg_upload_env(dpg_ctx *c, int32_t dim, const double *lo, const double *hi, int32_t n_obs,

@@ -139,8 +139,10 @@ __host__ __device__ constexpr size_t gemm_tma_smem_bytes(int N) {
   return (size_t)tma_stages(N) * (128 * 128 + N * 128) + 1024 + 256;
 }
 
+constexpr int kTmaThreads = 256;  // 8 warps: all of them drain the accumulator
+
 template <int N, class Epi>
-__global__ void __launch_bounds__(kGemmThreads) gemm_bf16_tma(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(kTmaThreads) gemm_bf16_tma(const __grid_constant__ CUtensorMap tmA,
                                                                const __grid_constant__ CUtensorMap tmB, int M,
                                                                int K, int k_per_split, Epi epi, int *err) {
   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "N");
@@ -225,14 +227,21 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_bf16_tma(const __grid_const
       for (int i = max(0, loads - S); i < loads; i++) umma::mbar_wait(&full[i % S], (i / S) & 1, 1u << 20);
     }
   } else if (nchunks > 0) {
-    umma::fence_after_sync();
-    const int row = 32 * warp + lane;
-    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+    // warp w reads accumulator lanes 32 (w % 4) ...; warps 0-3 and 4-7 split
+    // the columns in halves (all columns in warps 0-3 when N / 2 is not a
+    // multiple of 16)
+    constexpr int kHalves = (N % 32 == 0) ? 2 : 1, kNC = N / kHalves;
+    const int q = warp & 3, h = warp >> 2;
+    if (h < kHalves) {
+      umma::fence_after_sync();
+      const int row = 32 * q + lane;
+      const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
 #pragma unroll 1
-    for (int c0 = 0; c0 < N; c0 += 16) {
-      float v[16];
-      umma::tmem_ld16(lane_addr + c0, v);
-      if (m0 + row < M) epi(m0 + row, c0, v);
+      for (int c0 = h * kNC; c0 < (h + 1) * kNC; c0 += 16) {
+        float v[16];
+        umma::tmem_ld16(lane_addr + c0, v);
+        if (m0 + row < M) epi(m0 + row, c0, v);
+      }
     }
   }
   umma::fence_before_sync();
@@ -241,22 +250,48 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_bf16_tma(const __grid_const
 }
 
 // ---- epilogues ---------------------------------------------------------------
+// 16 consecutive FP32 values as four 16-byte stores (dst 16-byte aligned)
+__device__ __forceinline__ void store16(float *dst, const float *v) {
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+    reinterpret_cast<float4 *>(dst)[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+}
+__device__ __forceinline__ void load16(const float *src, float *v) {
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const float4 t = reinterpret_cast<const float4 *>(src)[j];
+    v[4 * j] = t.x; v[4 * j + 1] = t.y; v[4 * j + 2] = t.z; v[4 * j + 3] = t.w;
+  }
+}
+
 struct EpiStoreF32 {  // C = acc (ldc = row stride, only columns < n_valid)
   float *C;
   int ldc, n_valid;
   __device__ void operator()(int row, int c0, const float *v) const {
+    float *dst = C + (int64_t)row * ldc + c0;
+    if (c0 + 16 <= n_valid && (ldc & 3) == 0) {
+      store16(dst, v);
+      return;
+    }
 #pragma unroll
     for (int j = 0; j < 16; j++)
-      if (c0 + j < n_valid) C[(int64_t)row * ldc + c0 + j] = v[j];
+      if (c0 + j < n_valid) dst[j] = v[j];
   }
 };
 struct EpiAtomicF32 {  // C += acc (split-K partial sums)
   float *C;
   int ldc, n_valid;
   __device__ void operator()(int row, int c0, const float *v) const {
+    float *dst = C + (int64_t)row * ldc + c0;
+    if (c0 + 16 <= n_valid && (ldc & 3) == 0) {  // 16-byte vector atomics
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        atomicAdd(reinterpret_cast<float4 *>(dst) + j, make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]));
+      return;
+    }
 #pragma unroll
     for (int j = 0; j < 16; j++)
-      if (c0 + j < n_valid) atomicAdd(C + (int64_t)row * ldc + c0 + j, v[j]);
+      if (c0 + j < n_valid) atomicAdd(dst + j, v[j]);
   }
 };
 
@@ -276,12 +311,13 @@ struct EpiBiasGelu {
   int ld;
   __device__ void operator()(int row, int c0, const float *v) const {
     __align__(16) __nv_bfloat16 h[16];
+    float z[16];
+    load16(bias + c0, z);
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
-      const float z = v[j] + bias[c0 + j];
-      if (pre) pre[(int64_t)row * ld + c0 + j] = z;
-      h[j] = __float2bfloat16_rn(gelu(z));
-    }
+    for (int j = 0; j < 16; j++) z[j] += v[j];
+    if (pre) store16(pre + (int64_t)row * ld + c0, z);
+#pragma unroll
+    for (int j = 0; j < 16; j++) h[j] = __float2bfloat16_rn(gelu(z[j]));
     uint4 *dst = reinterpret_cast<uint4 *>(act + (int64_t)row * ld + c0);
     dst[0] = reinterpret_cast<const uint4 *>(h)[0];
     dst[1] = reinterpret_cast<const uint4 *>(h)[1];

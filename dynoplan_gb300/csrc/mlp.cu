@@ -57,7 +57,7 @@ cudaError_t launch_gemm_n(const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M,
     const size_t sm = gemm_tma_smem_bytes(N);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    kern<<<grid, kGemmThreads, sm, st>>>(ta, tb, M, K, per, epi, err);
+    kern<<<grid, kTmaThreads, sm, st>>>(ta, tb, M, K, per, epi, err);
     return cudaGetLastError();
   }
   auto kern = gemm_bf16_tn<N, Epi>;
@@ -408,8 +408,9 @@ int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *no
       e = launch_gemm(kMlpHidden, dz, M->WT16[l], (int)Bp, kMlpHidden, 1,
                       EpiGeluGrad{M->Z[l - 1], dz_next, kMlpHidden}, M->err, st);
     else
-      e = launch_gemm(kMlpIn, dz, M->WT16[0], (int)Bp, kMlpHidden, 1, EpiEmbGrad{prim_dev, M->g[DPG_MLP_EMB], B},
-                      M->err, st);
+      // only the embedding columns 80..95 of dX are needed: rows 80..95 of W1^T
+      e = launch_gemm(kMlpEmb, dz, M->WT16[0] + (size_t)kMlpNodeFeat * kMlpHidden, (int)Bp, kMlpHidden, 1,
+                      EpiEmbGrad{prim_dev, M->g[DPG_MLP_EMB], B}, M->err, st);
     std::swap(dz, dz_next);
   }
   if (e != cudaSuccess) return DPG_ERR_CUDA;

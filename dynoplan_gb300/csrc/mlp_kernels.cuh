@@ -140,23 +140,27 @@ struct EpiGeluGrad {
   int ld;
   __device__ void operator()(int row, int c0, const float *v) const {
     __align__(16) __nv_bfloat16 h[16];
+    float z[16];
+    load16(pre + (int64_t)row * ld + c0, z);
 #pragma unroll
-    for (int j = 0; j < 16; j++) h[j] = __float2bfloat16_rn(v[j] * gelu_grad(pre[(int64_t)row * ld + c0 + j]));
+    for (int j = 0; j < 16; j++) h[j] = __float2bfloat16_rn(v[j] * gelu_grad(z[j]));
     uint4 *dst = reinterpret_cast<uint4 *>(dz + (int64_t)row * ld + c0);
     dst[0] = reinterpret_cast<const uint4 *>(h)[0];
     dst[1] = reinterpret_cast<const uint4 *>(h)[1];
   }
 };
 
-// dE[prim[b]] += dX[b, 80:96]: the epilogue of dX = dZ1 * W1 (columns 80..95)
+// dE[prim[b]] += dX[b, 80:96]: the epilogue of the 16-column product
+// dZ1 * W1[:, 80:96] (the embedding part of the layer-1 input gradient)
 struct EpiEmbGrad {
   const uint32_t *prim;
   float *demb;
   int64_t B;
   __device__ void operator()(int row, int c0, const float *v) const {
-    if (c0 != kMlpNodeFeat || row >= B) return;
+    if (row >= B) return;
+    float4 *dst = reinterpret_cast<float4 *>(demb + (int64_t)prim[row] * kMlpEmb);
 #pragma unroll
-    for (int j = 0; j < 16; j++) atomicAdd(demb + (int64_t)prim[row] * kMlpEmb + (c0 - kMlpNodeFeat) + j, v[j]);
+    for (int j = 0; j < 4; j++) atomicAdd(dst + j, make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]));
   }
 };
 

@@ -109,6 +109,18 @@ class Context:
                                              _ptr(actions)), self.h)
         self.P = len(length)
 
+    def prepend_primitives(self, prims):
+        """Insert motions in front of the uploaded set (new indices 0..P-1,
+        the old ones shifted by P), as idbA* adds its optimised motions."""
+        length = np.ascontiguousarray(prims.length, dtype=np.int32)
+        states = np.ascontiguousarray(prims.states, dtype=np.float64)
+        actions = np.ascontiguousarray(prims.actions, dtype=np.float64)
+        if actions.size == 0:
+            actions = np.zeros((1, self.nu))
+        check(self.lib.dpg_prepend_primitives(self.h, len(length), _ptr(length), _ptr(states),
+                                              _ptr(actions)), self.h)
+        self.P = getattr(self, "P", 0) + len(length)
+
     def upload_env(self, env):
         lo = np.ascontiguousarray(env.lo, dtype=np.float64)
         hi = np.ascontiguousarray(env.hi, dtype=np.float64)

@@ -147,9 +147,21 @@ const char *dpg_last_error(const dpg_ctx *ctx);
  * nx doubles, concatenated) and len[p]-1 actions (rows of nu doubles).  The
  * index p is Motion::idx.  Replaces load_motion_primitives_new's tables and
  * the T_m tree build (src/ompl/robots.cpp:3061-3174, dbastar.cpp:564-575);
- * the noise and quaternion normalisation of the loader are the caller's. */
+ * the noise and quaternion normalisation of the loader are the caller's
+ * (dpg_primitives_prepare in dpg_prim_io.h). */
 int dpg_upload_primitives(dpg_ctx *ctx, int32_t P, const int32_t *len,
                           const double *states, const double *actions);
+
+/* Insert P motions (same layout) in front of the uploaded set and re-index:
+ * the new motions get indices 0..P-1, motion i of the old set becomes
+ * P + i.  Replaces idbA*'s add-primitives step (src/idbastar/idbastar.cpp:
+ * 234-291: motions.insert(motions.begin(), ...) then idx = position).  The
+ * old tables stay on the device (copied there, not re-sent); every derived
+ * table is rebuilt.  Equivalent to uploading the concatenation.  A surrogate
+ * (dpg_mlp.h) indexes primitives by position, so one trained before the
+ * insert no longer matches. */
+int dpg_prepend_primitives(dpg_ctx *ctx, int32_t P, const int32_t *len,
+                           const double *states, const double *actions);
 
 /* Upload the environment: state position bounds (dim values each) and
  * n_obs axis-aligned boxes (n_obs x dim corners).  Replaces load_env and the

@@ -67,6 +67,15 @@ def read_traj_yaml(path):
     return out, jumps
 
 
+def copy_bundled_msgpack(ref):
+    """the bundled unicycle1 file itself (81 kB), byte for byte: the reader's
+    and writer's format fixture"""
+    src = os.path.join(ref, "data/motion_primitives/unicycle1_v0/"
+                            "unicycle1_v0__ispso__2023_04_03__14_56_57.bin.less.bin.msgpack")
+    with open(src, "rb") as f, open(os.path.join(HERE, "unicycle1_bundled_primitives.msgpack"), "wb") as g:
+        g.write(f.read())
+
+
 def main(ref):
     # 1. bundled unicycle1 primitives
     d = read_msgpack(os.path.join(ref, "data/motion_primitives/unicycle1_v0/"
@@ -74,6 +83,7 @@ def main(ref):
     json.dump({"source": "data/motion_primitives/unicycle1_v0/unicycle1_v0__ispso__2023_04_03__14_56_57"
                          ".bin.less.bin.msgpack", "data": d["data"]},
               open(os.path.join(HERE, "unicycle1_bundled_primitives.json"), "w"))
+    copy_bundled_msgpack(ref)
 
     # 2. jump annotations (distance and lower_bound_time pins)
     jumps = {}
