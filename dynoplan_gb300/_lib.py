@@ -91,6 +91,7 @@ SIGNATURES = [
     ("dpg_mlp_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("dpg_mlp_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                      C.c_float, C.c_float, C.POINTER(C.c_float)]),
+    ("dpg_mlp_set_fused", C.c_int, [C.c_void_p, C.c_int]),
     ("dpg_mlp_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     # include/dpg_search.h
     ("dpg_search", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

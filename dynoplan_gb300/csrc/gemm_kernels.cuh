@@ -295,11 +295,24 @@ struct EpiAtomicF32 {  // C += acc (split-K partial sums)
   }
 };
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks & Gimpel, "Gaussian Error Linear Units",
+// 2016): gelu(z) = z/2 (1 + tanh(u)), u = sqrt(2/pi) (z + 0.044715 z^3), with
+// the hardware tanh (tanh.approx.f32, max relative error about 2^-11, below
+// the bf16 rounding the activations get).
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kGeluA = 0.7978845608028654f, kGeluB = 0.044715f;
+__device__ __forceinline__ float gelu(float z) {
+  const float t = tanh_fast(kGeluA * z * fmaf(kGeluB * z, z, 1.0f));
+  return 0.5f * z * (1.0f + t);
+}
 __device__ __forceinline__ float gelu_grad(float z) {
-  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * __expf(-0.5f * z * z);
-  return cdf + z * pdf;
+  const float t = tanh_fast(kGeluA * z * fmaf(kGeluB * z, z, 1.0f));
+  const float du = kGeluA * fmaf(3.0f * kGeluB * z, z, 1.0f);
+  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * du;
 }
 
 // z = acc + bias; keeps z (FP32, for the backward pass) when pre != nullptr;

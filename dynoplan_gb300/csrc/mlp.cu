@@ -142,6 +142,8 @@ struct dpg_mlp {
   float *Z[3] = {}, *out = nullptr, *loss = nullptr;
   int *err = nullptr;
   int step = 0;
+  int fused = 1;  // forward through mlp_forward_fused when the tensor maps can be made
+  int sm_count = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   double last_ms = 0, last_flops = 0;
 };
@@ -231,6 +233,7 @@ int dpg_mlp_create(dpg_mlp **out, int device, int n_prims, int64_t max_rows, uin
   dpg_mlp *M = new dpg_mlp();
   M->device = device;
   M->P = n_prims;
+  cudaDeviceGetAttribute(&M->sm_count, cudaDevAttrMultiProcessorCount, device);
   M->max_rows = max_rows;
   M->rows_pad = pad128(max_rows);
   const int64_t R = M->rows_pad;
@@ -343,7 +346,24 @@ int dpg_mlp_forward(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_
   cudaMemsetAsync(M->err, 0, sizeof(int), st);
   cudaEventRecord(M->e0, st);
   double flops = 0;
-  for (int64_t r0 = 0; r0 < n; r0 += M->max_rows) {
+  CUtensorMap tw[4];
+  const bool fused = M->fused && n > 0 && make_kmajor_map(&tw[0], M->W16[0], kMlpHidden, kMlpIn, kMlpHidden) &&
+                     make_kmajor_map(&tw[1], M->W16[1], kMlpHidden, kMlpHidden, kMlpHidden) &&
+                     make_kmajor_map(&tw[2], M->W16[2], kMlpHidden, kMlpHidden, kMlpHidden) &&
+                     make_kmajor_map(&tw[3], M->W16[3], kMlpOutPad, kMlpHidden, kMlpOutPad);
+  if (fused) {  // one persistent kernel, one CTA per SM
+    FusedArgs fa{nf, M->emb16, node_dev, prim_dev, M->w[DPG_MLP_B1], M->w[DPG_MLP_B2], M->w[DPG_MLP_B3],
+                 M->w[DPG_MLP_B4], out_dev, n, M->err};
+    if (cudaFuncSetAttribute(mlp_forward_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem) !=
+        cudaSuccess)
+      return DPG_ERR_CUDA;
+    const int64_t tiles = (n + 127) / 128;
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, std::max(M->sm_count, 1));
+    mlp_forward_fused<<<grid, kFusedThreads, kFusedSmem, st>>>(tw[0], tw[1], tw[2], tw[3], fa);
+    if (cudaGetLastError() != cudaSuccess) return DPG_ERR_CUDA;
+    flops = forward_flops(pad128(n));
+  }
+  for (int64_t r0 = 0; r0 < n && !fused; r0 += M->max_rows) {
     const int64_t B = std::min(M->max_rows, n - r0), Bp = pad128(B);
     const int64_t chunks = Bp * (kMlpIn / 8);
     mlp_assemble<<<(unsigned)((chunks + 255) / 256), 256, 0, st>>>(nf, M->emb16, node_dev + r0, prim_dev + r0, B, Bp,
@@ -435,6 +455,12 @@ int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *no
   // forward + the two backward GEMMs per layer
   M->last_flops = 3.0 * forward_flops(Bp);
   return check_err(M);
+}
+
+int dpg_mlp_set_fused(dpg_mlp *M, int fused) {
+  if (!M) return DPG_ERR_ARG;
+  M->fused = fused != 0;
+  return DPG_OK;
 }
 
 int dpg_mlp_last_timing(const dpg_mlp *M, double *ms, double *flops) {

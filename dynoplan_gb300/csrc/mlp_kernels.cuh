@@ -219,4 +219,200 @@ static __global__ void f32_to_bf16(const float *in, __nv_bfloat16 *out, int64_t 
   if (i < n) out[i] = __float2bfloat16_rn(in[i]);
 }
 
+// ---------------------------------------------------------------------------
+// Fused forward: the whole MLP for 128-row tiles in one persistent kernel.
+//
+// One CTA per SM (256 threads) walks tiles m0 = 128 * (blockIdx.x + k *
+// gridDim.x).  A tile's activations live in one 64 KB shared-memory buffer
+// (128 rows x 256 bf16, SW128 K-major): the gathered input [node features |
+// embedding | 0] first, then H1, H2, H3, each written over the previous
+// one once the layer's MMAs have read it.  Accumulators (128 x 256 FP32)
+// sit in TMEM; the epilogue adds the bias, applies GELU and writes bf16
+// back into the buffer.  W1..W3 stream by TMA in 64-column chunks (32 KB)
+// into four stages -- a whole layer -- while the previous epilogue runs;
+// W4 (16 x 256) stays resident.  Thread 0 issues every TMA and MMA.
+// Every wait is bounded: on expiry the kernel sets *err, drains its copies
+// and MMAs (bounded), frees TMEM and returns.
+struct FusedArgs {
+  const __nv_bfloat16 *node_feat, *emb;
+  const uint32_t *node, *prim;
+  const float *b1, *b2, *b3, *b4;
+  float *out;  // [B x 2]
+  int64_t B;
+  int *err;
+};
+constexpr int kFusedThreads = 256;
+constexpr uint32_t kActBytes = 128 * kMlpHidden * 2;        // 64 KB
+constexpr uint32_t kWChunk = kMlpHidden * 128;              // 256 rows x 64 bf16 = 32 KB
+constexpr uint32_t kW4Bytes = kMlpOutPad * kMlpHidden * 2;  // 8 KB
+constexpr size_t kFusedSmem = 1024 + kActBytes + 4 * kWChunk + kW4Bytes + 256;
+
+static __global__ void __launch_bounds__(kFusedThreads, 1)
+    mlp_forward_fused(const __grid_constant__ CUtensorMap tw1, const __grid_constant__ CUtensorMap tw2,
+                      const __grid_constant__ CUtensorMap tw3, const __grid_constant__ CUtensorMap tw4, FusedArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = umma::smem_u32(smem_raw);
+  unsigned char *act = smem_raw + ((1024 - (raw & 1023)) & 1023);
+  unsigned char *wst = act + kActBytes;           // 4 weight stages
+  unsigned char *w4 = wst + 4 * kWChunk;          // resident W4, 4 k-blocks of 16 rows
+  uint64_t *wfull = reinterpret_cast<uint64_t *>(w4 + kW4Bytes);  // [4]
+  uint64_t *w4full = wfull + 4;
+  uint64_t *done = w4full + 1;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t n_tiles = (a.B + 127) / 128;
+  const void *wmap[3] = {&tw1, &tw2, &tw3};
+  constexpr uint32_t kIdesc = umma::idesc_bf16_f32(128, kMlpHidden);
+  constexpr uint32_t kIdesc4 = umma::idesc_bf16_f32(128, kMlpOutPad);
+
+  if (tid == 0) {
+    for (int s = 0; s < 4; s++) umma::mbar_init(&wfull[s], 1);
+    umma::mbar_init(w4full, 1);
+    umma::mbar_init(done, 1);
+    umma::mbar_fence_init();
+  }
+  if (warp == 0) {
+    umma::tmem_alloc(tslot, 256);
+    umma::tmem_relinquish();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+
+  // thread 0's bookkeeping: phase of each weight stage, loads in flight
+  uint32_t wphase = 0;      // bit s: parity of the next completion of stage s
+  uint32_t inflight = 0;    // bit s: a load into stage s not yet waited for
+  uint32_t done_phase = 0;  // parity of the next `done` completion
+  bool w4_inflight = false;
+  auto load_layer = [&](int l) {  // all chunks of W(l+1), l = 0..2
+    const int chunks = (l == 0 ? kMlpIn : kMlpHidden) / 64;
+    for (int j = 0; j < chunks; j++) {
+      umma::mbar_arrive_expect_tx(&wfull[j], kWChunk);
+      umma::tma_load_2d(wst + j * kWChunk, wmap[l], 64 * j, 0, &wfull[j]);
+      inflight |= 1u << j;
+    }
+  };
+  if (tid == 0 && blockIdx.x < n_tiles) {
+    umma::mbar_arrive_expect_tx(w4full, kW4Bytes);
+    for (int j = 0; j < 4; j++) umma::tma_load_2d(w4 + j * (kMlpOutPad * 128), &tw4, 64 * j, 0, w4full);
+    w4_inflight = true;
+    load_layer(0);
+  }
+  bool w4_ready = false;
+  bool bad = false;  // this thread saw a wait expire; block-wide decisions use __syncthreads_or
+
+  for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int64_t m0 = t * 128;
+    // ---- gather the input rows into the buffer (k-blocks 0 and 1)
+    for (int i = tid; i < 128 * (kMlpIn / 8); i += kFusedThreads) {
+      const int r = i / (kMlpIn / 8), c = i % (kMlpIn / 8);
+      const int64_t b = m0 + r;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (b < a.B) {
+        if (c < kMlpNodeFeat / 8)
+          v = reinterpret_cast<const uint4 *>(a.node_feat + (int64_t)a.node[b] * kMlpNodeFeat)[c];
+        else if (c < (kMlpNodeFeat + kMlpEmb) / 8)
+          v = reinterpret_cast<const uint4 *>(a.emb + (int64_t)a.prim[b] * kMlpEmb)[c - kMlpNodeFeat / 8];
+      }
+      *reinterpret_cast<uint4 *>(act + umma::kmajor_offset(128, r, c)) = v;
+    }
+    umma::fence_proxy_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+
+    for (int l = 0; l < 4; l++) {
+      // ---- MMAs of layer l (thread 0)
+      if (tid == 0) {
+        umma::fence_after_sync();
+        const uint32_t a0 = umma::smem_u32(act);
+        if (l < 3) {
+          const int chunks = (l == 0 ? kMlpIn : kMlpHidden) / 64;
+          for (int j = 0; j < chunks && !bad; j++) {
+            if (!umma::mbar_wait(&wfull[j], (wphase >> j) & 1)) { bad = true; break; }
+            wphase ^= 1u << j;
+            inflight &= ~(1u << j);
+            umma::fence_after_sync();
+            const uint32_t b0 = umma::smem_u32(wst + j * kWChunk), ak = a0 + j * (128 * 128);
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+              umma::mma_bf16(tmem, umma::sdesc_kmajor_sw128(ak + kk * 32), umma::sdesc_kmajor_sw128(b0 + kk * 32),
+                             kIdesc, (j > 0 || kk > 0) ? 1u : 0u);
+          }
+        } else {
+          if (!w4_ready) {
+            if (umma::mbar_wait(w4full, 0)) {
+              w4_ready = true;
+              w4_inflight = false;
+            } else {
+              bad = true;
+            }
+          }
+          for (int j = 0; j < 4 && !bad; j++) {
+            const uint32_t b0 = umma::smem_u32(w4 + j * (kMlpOutPad * 128)), ak = a0 + j * (128 * 128);
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+              umma::mma_bf16(tmem, umma::sdesc_kmajor_sw128(ak + kk * 32), umma::sdesc_kmajor_sw128(b0 + kk * 32),
+                             kIdesc4, (j > 0 || kk > 0) ? 1u : 0u);
+          }
+        }
+        umma::commit(done);  // also after an expired wait: arrives once the issued MMAs are done
+      }
+      // ---- wait for the accumulator; refill the weight stages
+      if (umma::mbar_wait(done, done_phase)) done_phase ^= 1u;
+      else bad = true;
+      if (tid == 0 && !bad) {
+        if (l == 0) load_layer(1);
+        else if (l == 1) load_layer(2);
+        else if (l == 2 && t + gridDim.x < n_tiles) load_layer(0);  // the next tile's W1
+      }
+      umma::fence_after_sync();
+      // ---- epilogue: warps w and w + 4 share accumulator lanes 32 (w % 4)
+      const int q = warp & 3, h = warp >> 2, row = 32 * q + lane;
+      const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+      if (l < 3 && !bad) {
+        const float *bias = l == 0 ? a.b1 : (l == 1 ? a.b2 : a.b3);
+#pragma unroll 1
+        for (int c0 = 128 * h; c0 < 128 * (h + 1); c0 += 16) {
+          float v[16], z[16];
+          umma::tmem_ld16(lane_addr + c0, v);
+          load16(bias + c0, z);
+          __align__(16) __nv_bfloat16 hb[16];
+#pragma unroll
+          for (int j = 0; j < 16; j++) hb[j] = __float2bfloat16_rn(gelu(v[j] + z[j]));
+          *reinterpret_cast<uint4 *>(act + umma::kmajor_offset(128, row, c0 / 8)) =
+              reinterpret_cast<const uint4 *>(hb)[0];
+          *reinterpret_cast<uint4 *>(act + umma::kmajor_offset(128, row, c0 / 8 + 1)) =
+              reinterpret_cast<const uint4 *>(hb)[1];
+        }
+        umma::fence_proxy_async_smem();
+      } else if (l == 3 && !bad && h == 0) {
+        float v[16];
+        umma::tmem_ld16(lane_addr, v);
+        const int64_t b = m0 + row;
+        if (b < a.B) {
+          a.out[b * 2] = v[0] + a.b4[0];
+          a.out[b * 2 + 1] = v[1] + a.b4[1];
+        }
+      }
+      umma::fence_before_sync();
+      bad = __syncthreads_or(bad);  // the same decision in every thread
+      if (bad) break;
+    }
+    if (bad) break;
+  }
+  if (bad && tid == 0) {
+    atomicExch(a.err, 1);
+    // copies still in flight land, and MMAs finish, before the memory goes
+    for (int s = 0; s < 4; s++)
+      if (inflight & (1u << s)) umma::mbar_wait(&wfull[s], (wphase >> s) & 1, 1u << 20);
+    if (w4_inflight) umma::mbar_wait(w4full, 0, 1u << 20);
+    umma::mbar_wait(done, done_phase, 1u << 20);
+  }
+  if (!bad && tid == 0 && w4_inflight) umma::mbar_wait(w4full, 0, 1u << 20);  // no tile: W4 never used
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, 256);
+}
+
 }  // namespace dpg

@@ -86,6 +86,11 @@ class Surrogate:
                                           lr, ctg_weight, C.byref(loss)))
         return loss.value
 
+    def set_fused(self, fused: bool):
+        """forward through the fused per-tile kernel (default) or the
+        layer-by-layer GEMMs"""
+        check(self.lib.dpg_mlp_set_fused(self.h, 1 if fused else 0))
+
     def timing(self):
         ms, fl = C.c_double(), C.c_double()
         self.lib.dpg_mlp_last_timing(self.h, C.byref(ms), C.byref(fl))

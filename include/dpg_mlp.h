@@ -37,7 +37,8 @@ int dpg_gemm_bf16(const void *A_dev, const void *B_dev, float *C_dev, int M, int
 /* ---- the surrogate MLP --------------------------------------------------
  * Input row per (node, primitive) pair (96 bf16): normalised node state (16,
  * zero padded), 8x8 occupancy patch around the node (64), the primitive's
- * learned 16-D embedding.  Layers 96 -> 256 -> 256 -> 256 -> 2 with GELU;
+ * learned 16-D embedding.  Layers 96 -> 256 -> 256 -> 256 -> 2 with GELU
+ * (tanh form: z/2 (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))));
  * outputs [collision logit, cost-to-go].  BF16 weights and activations, FP32
  * accumulation (tcgen05), FP32 master weights, Adam. */
 typedef struct dpg_mlp dpg_mlp;
@@ -70,6 +71,13 @@ int dpg_mlp_forward(dpg_mlp *mlp, const void *node_feat_dev, const uint32_t *nod
 int dpg_mlp_train_step(dpg_mlp *mlp, const void *node_feat_dev, const uint32_t *node_dev,
                        const uint32_t *prim_dev, const float *target_dev, int64_t B, float lr, float ctg_weight,
                        float *loss);
+
+/* Forward kernels: fused != 0 (default) runs the whole MLP per 128-row tile
+ * in one persistent tcgen05 kernel (activations kept in shared memory,
+ * weights streamed by TMA); fused == 0 runs the layer-by-layer GEMMs the
+ * training step uses.  Same arithmetic (bf16 operands, FP32 accumulation in
+ * the same order, same epilogue). */
+int dpg_mlp_set_fused(dpg_mlp *mlp, int fused);
 
 /* device time of the last forward / train step (ms) and the FLOPs it ran */
 int dpg_mlp_last_timing(const dpg_mlp *mlp, double *ms, double *flops);

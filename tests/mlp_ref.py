@@ -3,7 +3,6 @@ with bf16 rounding at the same points as the GPU kernels (inputs, weights,
 hidden activations, loss gradient, pre-activation gradients).  Test
 infrastructure: the checker of dynoplan_gb300's MLP kernels."""
 import numpy as np
-from scipy.special import erf
 
 
 def bf16(x):
@@ -14,12 +13,17 @@ def bf16(x):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+GELU_A, GELU_B = np.sqrt(2.0 / np.pi), 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    """tanh form of GELU (Hendrycks & Gimpel 2016)"""
+    return 0.5 * z * (1.0 + np.tanh(GELU_A * (z + GELU_B * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+    t = np.tanh(GELU_A * (z + GELU_B * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_A * (1.0 + 3.0 * GELU_B * z * z)
 
 
 def assemble(node_feat, emb, node, prim):

@@ -101,3 +101,30 @@ def test_training_beats_random_order_on_held_out_envs(dpg_lib):
     rnd = np.mean([_checks_to_k_valid(rng.random(len(node)), node, valid, 5) for _ in range(3)])
     assert mlp_checks < 0.9 * rnd, (mlp_checks, rnd)
     m.close()
+
+
+@pytest.mark.parametrize("B", [1, 129, 5000, 300000])
+def test_fused_forward_matches_layer_by_layer(dpg_lib, B):
+    """the persistent fused forward (one CTA per SM walking 128-row tiles,
+    several tiles per CTA at the largest size) against the layer-by-layer
+    GEMMs: same bf16 operands and FP32 accumulation order"""
+    torch = pytest.importorskip("torch")
+    from dynoplan_gb300.surrogate import Surrogate
+    rng = np.random.default_rng(B + 7)
+    P, N = 64, 1000
+    params = _random_params(rng, P)
+    feat = rng.normal(0, 1, (N, 80)).astype(np.float32)
+    feat[:, 16:] = (rng.random((N, 64)) < 0.3)
+    dev = "cuda:0"
+    feat_d = torch.from_numpy(feat).to(dev).to(torch.bfloat16)
+    node_d = torch.from_numpy(rng.integers(0, N, B).astype(np.int32)).to(dev)
+    prim_d = torch.from_numpy(rng.integers(0, P, B).astype(np.int32)).to(dev)
+    s = Surrogate(P, max_rows=65536, seed=2)
+    for k, v in params.items():
+        s.set(k, v)
+    s.set_fused(False)
+    ref = s.forward(feat_d, node_d, prim_d).cpu().numpy()
+    s.set_fused(True)
+    out = s.forward(feat_d, node_d, prim_d).cpu().numpy()
+    assert out.shape == (B, 2) and np.isfinite(out).all()
+    assert np.abs(out - ref).max() <= 1e-3 * (1 + np.abs(ref).max())
