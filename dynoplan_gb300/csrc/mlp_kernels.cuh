@@ -222,7 +222,7 @@ static __global__ void f32_to_bf16(const float *in, __nv_bfloat16 *out, int64_t 
 // ---------------------------------------------------------------------------
 // Fused forward: the whole MLP for 128-row tiles in one persistent kernel.
 //
-// One CTA per SM (256 threads) walks tiles m0 = 128 * (blockIdx.x + k *
+// One CTA per SM (512 threads) walks tiles m0 = 128 * (blockIdx.x + k *
 // gridDim.x).  A tile's activations live in one 64 KB shared-memory buffer
 // (128 rows x 256 bf16, SW128 K-major): the gathered input [node features |
 // embedding | 0] first, then H1, H2, H3, each written over the previous
@@ -241,7 +241,7 @@ struct FusedArgs {
   int64_t B;
   int *err;
 };
-constexpr int kFusedThreads = 256;
+constexpr int kFusedThreads = 512;  // 16 warps: 4 per accumulator lane quarter
 constexpr uint32_t kActBytes = 128 * kMlpHidden * 2;        // 64 KB
 constexpr uint32_t kWChunk = kMlpHidden * 128;              // 256 rows x 64 bf16 = 32 KB
 constexpr uint32_t kW4Bytes = kMlpOutPad * kMlpHidden * 2;  // 8 KB
@@ -261,6 +261,9 @@ static __global__ void __launch_bounds__(kFusedThreads, 1)
   uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t n_tiles = (a.B + 127) / 128;
+  __shared__ __align__(16) float sbias[3][kMlpHidden];  // b1..b3, read by the epilogues
+  for (int i = tid; i < 3 * kMlpHidden; i += kFusedThreads)
+    sbias[i / kMlpHidden][i % kMlpHidden] = (i < kMlpHidden ? a.b1 : (i < 2 * kMlpHidden ? a.b2 : a.b3))[i % kMlpHidden];
   const void *wmap[3] = {&tw1, &tw2, &tw3};
   constexpr uint32_t kIdesc = umma::idesc_bf16_f32(128, kMlpHidden);
   constexpr uint32_t kIdesc4 = umma::idesc_bf16_f32(128, kMlpOutPad);
@@ -367,23 +370,24 @@ static __global__ void __launch_bounds__(kFusedThreads, 1)
         else if (l == 2 && t + gridDim.x < n_tiles) load_layer(0);  // the next tile's W1
       }
       umma::fence_after_sync();
-      // ---- epilogue: warps w and w + 4 share accumulator lanes 32 (w % 4)
+      // ---- epilogue: warps w, w + 4, w + 8, w + 12 share accumulator lanes
+      // 32 (w % 4), 64 columns each
       const int q = warp & 3, h = warp >> 2, row = 32 * q + lane;
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
       if (l < 3 && !bad) {
-        const float *bias = l == 0 ? a.b1 : (l == 1 ? a.b2 : a.b3);
+        const float *bias = sbias[l];
 #pragma unroll 1
-        for (int c0 = 128 * h; c0 < 128 * (h + 1); c0 += 16) {
-          float v[16], z[16];
-          umma::tmem_ld16(lane_addr + c0, v);
-          load16(bias + c0, z);
-          __align__(16) __nv_bfloat16 hb[16];
+        for (int c0 = 64 * h; c0 < 64 * (h + 1); c0 += 32) {
+          float v[32];
+          umma::tmem_ld32(lane_addr + c0, v);
+          __align__(16) __nv_bfloat162 hb[16];
 #pragma unroll
-          for (int j = 0; j < 16; j++) hb[j] = __float2bfloat16_rn(gelu(v[j] + z[j]));
-          *reinterpret_cast<uint4 *>(act + umma::kmajor_offset(128, row, c0 / 8)) =
-              reinterpret_cast<const uint4 *>(hb)[0];
-          *reinterpret_cast<uint4 *>(act + umma::kmajor_offset(128, row, c0 / 8 + 1)) =
-              reinterpret_cast<const uint4 *>(hb)[1];
+          for (int j = 0; j < 16; j++)
+            hb[j] = __floats2bfloat162_rn(gelu(v[2 * j] + bias[c0 + 2 * j]), gelu(v[2 * j + 1] + bias[c0 + 2 * j + 1]));
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            *reinterpret_cast<uint4 *>(act + umma::kmajor_offset(128, row, c0 / 8 + k)) =
+                reinterpret_cast<const uint4 *>(hb)[k];
         }
         umma::fence_proxy_async_smem();
       } else if (l == 3 && !bad && h == 0) {

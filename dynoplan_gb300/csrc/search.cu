@@ -146,33 +146,113 @@ __device__ double full_dist64(const RobotParams &rp, const double *a, const doub
   }
 }
 
-// block y = query; threads stride over targets.  Targets are rows of nx
-// doubles (FP64) mirrored as FP32.  lower_only: only targets t < q (a query
-// set against itself).  Up to K ids per query (count may exceed K).
+// ---- novelty radius query through a uniform grid over position ----------
+// Every metric here is >= w0 * |position difference|, so a target within
+// `radius` lies in the query's cell or a neighbouring one when the cell side
+// is radius / w0 (slightly enlarged for rounding).  Each round the targets
+// are counting-sorted by cell (count, scan, scatter); a warp per query scans
+// the 3^POSD neighbouring cells' contiguous ranges.  Neighbour lists are
+// sorted on the host, so the order within a cell does not matter.
+struct Grid {
+  float lo[3];
+  float inv_cs;
+  int n[3];
+};
+
 template <int KIND>
-__global__ void radius_query(RobotParams rp, float4 w32, const double *q64, const float *q32, int Q, int q_off,
-                             const double *t64, const float *t32, int T, double radius, float band, int lower_only,
-                             int K, int *count, int *ids) {
+__device__ __forceinline__ int grid_coord(const Grid &g, const float *x, int d) {
+  const int c = (int)floorf((x[d] - g.lo[d]) * g.inv_cs);
+  return min(max(c, 0), g.n[d] - 1);
+}
+
+template <int KIND>
+__global__ void grid_count(Grid g, const float *rows, int n, int *cell_of, int *cnt) {
   using R = Robot<KIND>;
-  const int q = blockIdx.y + q_off;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *x = rows + (int64_t)i * R::NX;
+  int c = grid_coord<KIND>(g, x, 0) + g.n[0] * grid_coord<KIND>(g, x, 1);
+  if (R::POSD == 3) c += g.n[0] * g.n[1] * grid_coord<KIND>(g, x, 2);
+  cell_of[i] = c;
+  atomicAdd(&cnt[c], 1);
+}
+
+// single block: start = exclusive prefix of cnt over n_cells cells
+static __global__ void __launch_bounds__(1024) grid_scan(int n_cells, const int *cnt, int *start) {
+  __shared__ int part[1024];
+  const int t = threadIdx.x, per = (n_cells + 1023) / 1024;
+  const int b = min(n_cells, t * per), e = min(n_cells, b + per);
+  int sum = 0;
+  for (int i = b; i < e; i++) sum += cnt[i];
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int run = part[t] - sum;
+  for (int i = b; i < e; i++) {
+    start[i] = run;
+    run += cnt[i];
+  }
+}
+
+static __global__ void grid_scatter(int n, const int *cell_of, const int *start, int *fill, int *sorted) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = cell_of[i];
+  sorted[start[c] + atomicAdd(&fill[c], 1)] = i;
+}
+
+// warp per query over the neighbouring cells (lower_only: targets t < q).
+// Count pass (offset == nullptr): count[q] = neighbours; write pass: the
+// neighbour ids packed at ids[offset[q] ...].
+template <int KIND>
+__global__ void grid_query(RobotParams rp, float4 w32, Grid g, const double *q64, const float *q32, int Q,
+                           const double *t64, const float *t32, const int *start, const int *cnt, const int *sorted,
+                           double radius, float band, int lower_only, const int64_t *offset, int *count, int *ids) {
+  using R = Robot<KIND>;
+  const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (q >= Q) return;
   float a[R::NX];
 #pragma unroll
   for (int i = 0; i < R::NX; i++) a[i] = q32[(int64_t)q * R::NX + i];
-  const int tend = lower_only ? min(T, q) : T;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tend; t += gridDim.x * blockDim.x) {
-    float b[R::NX];
+  int c0[3] = {0, 0, 0};
 #pragma unroll
-    for (int i = 0; i < R::NX; i++) b[i] = t32[(int64_t)t * R::NX + i];
-    const float d = full_dist32<KIND>(w32, a, b);
-    bool in = d <= (float)radius;
-    if (fabsf(d - (float)radius) <= band)
-      in = full_dist64<KIND>(rp, q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX) <= radius;
-    if (in) {
-      const int slot = atomicAdd(&count[q], 1);
-      if (slot < K) ids[(int64_t)q * K + slot] = t;
-    }
-  }
+  for (int d = 0; d < R::POSD; d++) c0[d] = grid_coord<KIND>(g, a, d);
+  int n_in = 0;
+  const int zr = R::POSD == 3 ? 1 : 0;
+  for (int dz = -zr; dz <= zr; dz++)
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) {
+        const int cx = c0[0] + dx, cy = c0[1] + dy, cz = c0[2] + dz;
+        if (cx < 0 || cy < 0 || cz < 0 || cx >= g.n[0] || cy >= g.n[1] || (R::POSD == 3 && cz >= g.n[2])) continue;
+        const int cell = cx + g.n[0] * (cy + g.n[1] * cz);
+        const int s = start[cell], e = s + cnt[cell];
+        for (int j = s; j < e; j += 32) {
+          const int i = j + lane;
+          bool in = false;
+          int t = 0;
+          if (i < e) {
+            t = sorted[i];
+            if (!(lower_only && t >= q)) {
+              float b[R::NX];
+#pragma unroll
+              for (int k = 0; k < R::NX; k++) b[k] = t32[(int64_t)t * R::NX + k];
+              const float d = full_dist32<KIND>(w32, a, b);
+              in = d <= (float)radius;
+              if (fabsf(d - (float)radius) <= band)
+                in = full_dist64<KIND>(rp, q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX) <= radius;
+            }
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, in);
+          if (in && offset) ids[offset[q] + n_in + __popc(m & ((1u << lane) - 1u))] = t;
+          n_in += __popc(m);
+        }
+      }
+  if (lane == 0 && !offset) count[q] = n_in;
 }
 
 template <class F> void with_kind_s(int kind, F &&f) {
@@ -253,7 +333,6 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   if (rc) return rc;
   const double goal_tol = o->delta_factor_goal * o->delta;
   const double nov_radius = (1.0 - o->alpha) * o->delta;
-  int Kq = std::max(1, o->max_neighbors);  // neighbour-id capacity per query
   std::mt19937 rng((uint32_t)o->seed);
 
   // explored nodes (host) + their states mirrored on the GPU for the queries
@@ -266,6 +345,39 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
     xs.insert(xs.end(), x, x + nx);
     return (int)nodes.size() - 1;
   };
+  // novelty grid over position: cell side = radius / w0 (slightly enlarged),
+  // at most 256 cells a side in 2-D and 40 in 3-D
+  Grid grid{};
+  int n_cells = 1;
+  {
+    const int pd = r.kind == DPG_ROBOT_QUAD3D ? 3 : 2;
+    double cs = nov_radius / std::max(r.w[0], 1e-12) * (1.0 + 1e-5) + 1e-6;
+    for (int d = 0; d < pd; d++) cs = std::max(cs, (c->hi[d] - c->lo[d]) / (pd == 3 ? 40.0 : 256.0));
+    grid.inv_cs = (float)(1.0 / cs);
+    for (int d = 0; d < 3; d++) {
+      grid.lo[d] = (float)c->lo[d];
+      grid.n[d] = d < pd ? std::max(1, (int)std::ceil((c->hi[d] - c->lo[d]) / cs)) : 1;
+      n_cells *= grid.n[d];
+    }
+  }
+  // cell-sorted copies of the explored nodes (t_*) and of a round's successors (s_*)
+  DVec<int> tab_cnt, tab_start, tab_fill, tab_cell, tab_sorted, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted;
+  if (!tab_cnt.reserve(n_cells) || !tab_start.reserve(n_cells) || !tab_fill.reserve(n_cells) ||
+      !rnd_cnt.reserve(n_cells) || !rnd_start.reserve(n_cells) || !rnd_fill.reserve(n_cells))
+    return DPG_ERR_OOM;
+  auto sort_by_cell = [&](const float *rows, int n, DVec<int> &cnt, DVec<int> &start, DVec<int> &fill,
+                          DVec<int> &cell, DVec<int> &sorted) -> bool {
+    if (!cell.reserve(std::max(n, 1)) || !sorted.reserve(std::max(n, 1))) return false;
+    cudaMemset(cnt.p, 0, sizeof(int) * n_cells);
+    cudaMemset(fill.p, 0, sizeof(int) * n_cells);
+    with_kind_s(r.kind, [&](auto Kd) {
+      constexpr int KIND = decltype(Kd)::value;
+      if (n > 0) grid_count<KIND><<<(n + 255) / 256, 256>>>(grid, rows, n, cell.p, cnt.p);
+      grid_scan<<<1, 1024>>>(n_cells, cnt.p, start.p);
+      if (n > 0) grid_scatter<<<(n + 255) / 256, 256>>>(n, cell.p, start.p, fill.p, sorted.p);
+    });
+    return true;
+  };
   size_t uploaded = 0;
   auto sync_table = [&]() -> bool {
     const size_t n = nodes.size();
@@ -276,6 +388,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
                  cudaMemcpyHostToDevice);
       cudaMemcpy(t32.p + uploaded * nx, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice);
       uploaded = n;
+      return sort_by_cell(t32.p, (int)n, tab_cnt, tab_start, tab_fill, tab_cell, tab_sorted);
     }
     return true;
   };
@@ -296,6 +409,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   DVec<double> q64, b64;
   DVec<float> q32;
   DVec<int> cnt_tab, ids_tab, cnt_self, ids_self;
+  DVec<int64_t> off_tab, off_self;
   DVec<uint32_t> pnode, pprim;
   DVec<float> mlp_out;
   DVec<__nv_bfloat16> feat;
@@ -434,36 +548,45 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       std::vector<float> qf(c_x.begin(), c_x.end());
       cudaMemcpy(q64.p, c_x.data(), sizeof(double) * c_x.size(), cudaMemcpyHostToDevice);
       cudaMemcpy(q32.p, qf.data(), sizeof(float) * qf.size(), cudaMemcpyHostToDevice);
-      const int T = (int)nodes.size();
+      // the round's successors sorted by cell too, for the lower-index query
+      if (!sort_by_cell(q32.p, Q, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted)) return DPG_ERR_OOM;
+      // count pass, offsets on the host, write pass into packed lists
       std::vector<int> ct(Q), cs(Q), it, is;
-      for (;;) {
-        if (!ids_tab.reserve((size_t)Q * Kq) || !ids_self.reserve((size_t)Q * Kq)) return DPG_ERR_OOM;
-        cudaMemset(cnt_tab.p, 0, sizeof(int) * Q);
-        cudaMemset(cnt_self.p, 0, sizeof(int) * Q);
+      std::vector<int64_t> ot(Q), os(Q);
+      const unsigned qblocks = (unsigned)((Q + 7) / 8);  // 8 warps of 32 lanes, a warp per query
+      auto query = [&](const int64_t *off_t, const int64_t *off_s) {
         with_kind_s(r.kind, [&](auto Kd) {
           constexpr int KIND = decltype(Kd)::value;
-          for (int q0 = 0; q0 < Q; q0 += 65535) {  // grid.y limit
-            const int nq = std::min(65535, Q - q0);
-            dim3 g1((unsigned)std::min(64, (T + 255) / 256), (unsigned)nq);
-            radius_query<KIND><<<g1, 256>>>(c->rp, w32, q64.p, q32.p, Q, q0, t64.p, t32.p, T, nov_radius, 1e-5f, 0,
-                                            Kq, cnt_tab.p, ids_tab.p);
-            dim3 g2((unsigned)std::min(64, (Q + 255) / 256), (unsigned)nq);
-            radius_query<KIND><<<g2, 256>>>(c->rp, w32, q64.p, q32.p, Q, q0, q64.p, q32.p, Q, nov_radius, 1e-5f, 1,
-                                            Kq, cnt_self.p, ids_self.p);
-          }
+          grid_query<KIND><<<qblocks, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, t64.p, t32.p, tab_start.p,
+                                             tab_cnt.p, tab_sorted.p, nov_radius, 1e-5f, 0, off_t, cnt_tab.p,
+                                             ids_tab.p);
+          grid_query<KIND><<<qblocks, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, q64.p, q32.p, rnd_start.p,
+                                             rnd_cnt.p, rnd_sorted.p, nov_radius, 1e-5f, 1, off_s, cnt_self.p,
+                                             ids_self.p);
         });
-        cudaMemcpy(ct.data(), cnt_tab.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
-        if (cudaMemcpy(cs.data(), cnt_self.p, sizeof(int) * Q, cudaMemcpyDeviceToHost) != cudaSuccess)
-          return DPG_ERR_CUDA;
-        const int maxc = std::max(*std::max_element(ct.begin(), ct.end()), *std::max_element(cs.begin(), cs.end()));
-        if (maxc <= Kq) break;
-        Kq = maxc;
-      }
-      it.resize((size_t)Q * Kq);
-      is.resize((size_t)Q * Kq);
-      cudaMemcpy(it.data(), ids_tab.p, sizeof(int) * it.size(), cudaMemcpyDeviceToHost);
-      if (cudaMemcpy(is.data(), ids_self.p, sizeof(int) * is.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+      };
+      query(nullptr, nullptr);
+      cudaMemcpy(ct.data(), cnt_tab.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
+      if (cudaMemcpy(cs.data(), cnt_self.p, sizeof(int) * Q, cudaMemcpyDeviceToHost) != cudaSuccess)
         return DPG_ERR_CUDA;
+      int64_t nt = 0, ns = 0;
+      for (int i = 0; i < Q; i++) {
+        ot[i] = nt;
+        os[i] = ns;
+        nt += ct[i];
+        ns += cs[i];
+      }
+      if (!ids_tab.reserve((size_t)std::max<int64_t>(nt, 1)) || !ids_self.reserve((size_t)std::max<int64_t>(ns, 1)) ||
+          !off_tab.reserve(Q) || !off_self.reserve(Q))
+        return DPG_ERR_OOM;
+      cudaMemcpy(off_tab.p, ot.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice);
+      cudaMemcpy(off_self.p, os.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice);
+      query(off_tab.p, off_self.p);
+      it.resize((size_t)nt);
+      is.resize((size_t)ns);
+      if (nt) cudaMemcpy(it.data(), ids_tab.p, sizeof(int) * nt, cudaMemcpyDeviceToHost);
+      if (ns) cudaMemcpy(is.data(), ids_self.p, sizeof(int) * ns, cudaMemcpyDeviceToHost);
+      if (cudaGetLastError() != cudaSuccess) return DPG_ERR_CUDA;
       res->novelty_ms += elapsed_ms() - tn0;
 
       // learned heuristic: the surrogate's cost-to-go of every (node, motion)
@@ -492,9 +615,9 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
           if (o->heuristic == DPG_HEU_MLP) h = std::max(h, kCtgScale * std::max(0.0, (double)pred[2 * (size_t)ci + 1]));
           const double g = (double)nodes[parent].g + c_cost[ci] +
                            o->cost_delta_factor * lower_bound_time(r, &xs[(size_t)parent * nx], &c_x0[(size_t)ci * nx]);
-          nbr.assign(it.begin() + (size_t)ci * Kq, it.begin() + (size_t)ci * Kq + ct[ci]);
+          nbr.assign(it.begin() + ot[ci], it.begin() + ot[ci] + ct[ci]);
           for (int k = 0; k < cs[ci]; k++) {
-            const int other = is[(size_t)ci * Kq + k];
+            const int other = is[os[ci] + k];
             if (accepted_as[other] >= 0) nbr.push_back(accepted_as[other]);
           }
           std::sort(nbr.begin(), nbr.end());

@@ -16,9 +16,11 @@
  * at the limit, so successors are prepared in rounds: each unfinished node,
  * in pop order, visits its next chunk of valid motions (2 x the limit,
  * doubling per round) until it has `limit` new nodes.  The novelty queries
- * of a round run as one brute-force radius query on the GPU (FP32 with an
- * FP64 re-test near the radius; neighbour lists are complete, whatever
- * their length); insertion and rewiring run on the host in that order.
+ * of a round run on the GPU through a uniform grid over position (cell side
+ * radius / position weight, nodes counting-sorted by cell, a warp per query
+ * over the neighbouring cells; FP32 with an FP64 re-test near the radius);
+ * neighbour lists are complete: counted, then packed.  Insertion and
+ * rewiring run on the host in that order.
  * batch = 1 visits nodes and motions in the reference's order.
  */
 #ifndef DPG_SEARCH_H
@@ -58,8 +60,8 @@ typedef struct dpg_search_opts {
   int32_t shuffle;                /* 1: shuffle each node's candidates (std::mt19937 seeded
                                      with `seed`, then std::shuffle, as expand_lazy);
                                      0: ascending motion index */
-  int32_t max_neighbors;          /* initial neighbour-list capacity per successor (it grows
-                                     to the largest neighbour count; lists are complete) */
+  int32_t max_neighbors;          /* unused (kept for layout): neighbour lists are complete,
+                                     counted then packed on the GPU */
   uint64_t seed;
 } dpg_search_opts;
 
