@@ -55,15 +55,15 @@ cudaError_t launch_gemm_n(const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M,
   if (tma && make_kmajor_map(&ta, A, (uint64_t)M, (uint64_t)K, 128) && make_kmajor_map(&tb, B, N, (uint64_t)K, N)) {
     auto kern = gemm_bf16_tma<N, Epi>;
     const size_t sm = gemm_tma_smem_bytes(N);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
+    static cudaError_t attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (attr != cudaSuccess) return attr;
     kern<<<grid, kTmaThreads, sm, st>>>(ta, tb, M, K, per, epi, err);
     return cudaGetLastError();
   }
   auto kern = gemm_bf16_tn<N, Epi>;
   const size_t sm = gemm_smem_bytes(N);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
+  static cudaError_t attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (attr != cudaSuccess) return attr;
   kern<<<grid, kGemmThreads, sm, st>>>(A, B, M, K, per, epi, err);
   return cudaGetLastError();
 }
@@ -144,6 +144,14 @@ struct dpg_mlp {
   int step = 0;
   int fused = 1;  // forward through mlp_forward_fused when the tensor maps can be made
   int sm_count = 0;
+  // training-step inputs copied to fixed buffers, hyper-parameters in device
+  // memory [lr, ctg_weight, 1 - b1^t, 1 - b2^t]: the step is captured once
+  // per (batch size, feature table) as a CUDA graph and replayed
+  uint32_t *in_node = nullptr, *in_prim = nullptr;
+  float *in_target = nullptr, *hp = nullptr, *hp_host = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int64_t graph_B = -1;
+  const void *graph_feat = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   double last_ms = 0, last_flops = 0;
 };
@@ -259,6 +267,9 @@ int dpg_mlp_create(dpg_mlp **out, int device, int n_prims, int64_t max_rows, uin
   for (int l = 0; l < 3 && ok; l++)
     ok = dalloc(&M->H[l], (size_t)R * kMlpHidden) == cudaSuccess && dalloc(&M->Z[l], (size_t)R * kMlpHidden) == cudaSuccess;
   ok = ok && cudaEventCreate(&M->e0) == cudaSuccess && cudaEventCreate(&M->e1) == cudaSuccess;
+  ok = ok && dalloc(&M->in_node, R) == cudaSuccess && dalloc(&M->in_prim, R) == cudaSuccess &&
+       dalloc(&M->in_target, 2 * R) == cudaSuccess && dalloc(&M->hp, 4) == cudaSuccess &&
+       cudaHostAlloc(&M->hp_host, 4 * sizeof(float), cudaHostAllocDefault) == cudaSuccess;
   if (!ok) {
     dpg_mlp_destroy(M);
     return DPG_ERR_OOM;
@@ -306,8 +317,11 @@ void dpg_mlp_destroy(dpg_mlp *M) {
     cudaFree(M->H[l]);
     cudaFree(M->Z[l]);
   }
-  void *bufs[] = {M->emb16, M->X, M->dZa, M->dZb, M->dY, M->T1, M->T2, M->out, M->loss, M->err};
+  void *bufs[] = {M->emb16, M->X,   M->dZa,     M->dZb,     M->dY,     M->T1,  M->T2,
+                  M->out,   M->loss, M->err, M->in_node, M->in_prim, M->in_target, M->hp};
   for (void *b : bufs) cudaFree(b);
+  if (M->hp_host) cudaFreeHost(M->hp_host);
+  if (M->graph) cudaGraphExecDestroy(M->graph);
   if (M->e0) cudaEventDestroy(M->e0);
   if (M->e1) cudaEventDestroy(M->e1);
   if (M->stream) cudaStreamDestroy(M->stream);
@@ -380,22 +394,21 @@ int dpg_mlp_forward(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_
   return check_err(M);
 }
 
-int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_dev, const uint32_t *prim_dev,
-                       const float *target_dev, int64_t B, float lr, float ctg_weight, float *loss) {
-  if (!M || !node_feat_dev || !node_dev || !prim_dev || !target_dev || B <= 0 || B > M->max_rows) return DPG_ERR_ARG;
-  cudaSetDevice(M->device);
-  cudaStream_t st = M->stream;
+}  // extern "C"
+
+// Every device operation of one training step, reading the batch from the
+// fixed input buffers and the hyper-parameters from M->hp (capturable).
+static cudaError_t enqueue_train(dpg_mlp *M, const __nv_bfloat16 *nf, int64_t B, cudaStream_t st) {
   const int64_t Bp = pad128(B);
   const int split = (int)std::max<int64_t>(1, std::min<int64_t>(64, Bp / 1024));
   cudaMemsetAsync(M->err, 0, sizeof(int), st);
   cudaMemsetAsync(M->loss, 0, sizeof(float), st);
   for (int i = 0; i < DPG_MLP_NPARAM; i++) cudaMemsetAsync(M->g[i], 0, sizeof(float) * M->n[i], st);
-  cudaEventRecord(M->e0, st);
-  const auto *nf = static_cast<const __nv_bfloat16 *>(node_feat_dev);
   const int64_t chunks = Bp * (kMlpIn / 8);
-  mlp_assemble<<<(unsigned)((chunks + 255) / 256), 256, 0, st>>>(nf, M->emb16, node_dev, prim_dev, B, Bp, M->X);
-  if (forward_rows(M, B, true, M->out, st) != cudaSuccess) return DPG_ERR_CUDA;
-  mlp_loss<<<(unsigned)((Bp + 255) / 256), 256, 0, st>>>(M->out, target_dev, B, Bp, ctg_weight, M->dY, M->loss);
+  mlp_assemble<<<(unsigned)((chunks + 255) / 256), 256, 0, st>>>(nf, M->emb16, M->in_node, M->in_prim, B, Bp, M->X);
+  cudaError_t e = forward_rows(M, B, true, M->out, st);
+  if (e != cudaSuccess) return e;
+  mlp_loss<<<(unsigned)((Bp + 255) / 256), 256, 0, st>>>(M->out, M->in_target, B, Bp, M->hp, M->dY, M->loss);
   dim3 tb(32, 8);
   auto transpose = [&](const __nv_bfloat16 *in, __nv_bfloat16 *o, int64_t rows, int64_t cols) {
     dim3 tg((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
@@ -405,7 +418,6 @@ int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *no
     dim3 g((ncol + 31) / 32, 64), b(32, 8);
     column_sums_bf16<<<g, b, 0, st>>>(in, Bp, ld, ncol, o);
   };
-  cudaError_t e = cudaSuccess;
   // layer 4: dW4 = dY^T H3 (16 rows), db4, dZ3 = (dY W4) * gelu'(Z3)
   transpose(M->dY, M->T1, Bp, kDY);
   transpose(M->H[2], M->T2, Bp, kMlpHidden);
@@ -430,19 +442,62 @@ int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *no
     else
       // only the embedding columns 80..95 of dX are needed: rows 80..95 of W1^T
       e = launch_gemm(kMlpEmb, dz, M->WT16[0] + (size_t)kMlpNodeFeat * kMlpHidden, (int)Bp, kMlpHidden, 1,
-                      EpiEmbGrad{prim_dev, M->g[DPG_MLP_EMB], B}, M->err, st);
+                      EpiEmbGrad{M->in_prim, M->g[DPG_MLP_EMB], B}, M->err, st);
     std::swap(dz, dz_next);
   }
-  if (e != cudaSuccess) return DPG_ERR_CUDA;
-  // Adam
-  M->step++;
-  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-  const float bc1 = 1.f - powf(b1, (float)M->step), bc2 = 1.f - powf(b2, (float)M->step);
+  if (e != cudaSuccess) return e;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;  // Adam
   for (int i = 0; i < DPG_MLP_NPARAM; i++) {
     const int64_t n = M->n[i];
-    adam_update<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(M->w[i], M->g[i], M->m[i], M->v[i], n, lr, b1, b2,
-                                                             eps, bc1, bc2, nullptr, nullptr, 0, 1);
+    adam_update<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(M->w[i], M->g[i], M->m[i], M->v[i], n, M->hp, b1, b2,
+                                                             eps, nullptr, nullptr, 0, 1);
     refresh_bf16(M, i, st);
+  }
+  return cudaGetLastError();
+}
+
+extern "C" {
+
+int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_dev, const uint32_t *prim_dev,
+                       const float *target_dev, int64_t B, float lr, float ctg_weight, float *loss) {
+  if (!M || !node_feat_dev || !node_dev || !prim_dev || !target_dev || B <= 0 || B > M->max_rows) return DPG_ERR_ARG;
+  cudaSetDevice(M->device);
+  cudaStream_t st = M->stream;
+  const auto *nf = static_cast<const __nv_bfloat16 *>(node_feat_dev);
+  // this step's batch and hyper-parameters into the fixed buffers
+  M->step++;
+  M->hp_host[0] = lr;
+  M->hp_host[1] = ctg_weight;
+  M->hp_host[2] = 1.f - powf(0.9f, (float)M->step);
+  M->hp_host[3] = 1.f - powf(0.999f, (float)M->step);
+  cudaMemcpyAsync(M->in_node, node_dev, sizeof(uint32_t) * B, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(M->in_prim, prim_dev, sizeof(uint32_t) * B, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(M->in_target, target_dev, sizeof(float) * 2 * B, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(M->hp, M->hp_host, 4 * sizeof(float), cudaMemcpyHostToDevice, st);
+  // the step as a CUDA graph, captured on first use for this batch size and
+  // feature table; without a graph (capture refused) the step runs eagerly
+  if (!(M->graph && M->graph_B == B && M->graph_feat == nf)) {
+    if (M->graph) cudaGraphExecDestroy(M->graph);
+    M->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const cudaError_t e = enqueue_train(M, nf, B, st);
+      const cudaError_t ee = cudaStreamEndCapture(st, &g);
+      if (e == cudaSuccess && ee == cudaSuccess && g && cudaGraphInstantiate(&M->graph, g, 0) == cudaSuccess) {
+        M->graph_B = B;
+        M->graph_feat = nf;
+      } else {
+        M->graph = nullptr;
+      }
+      if (g) cudaGraphDestroy(g);
+    }
+    cudaGetLastError();  // a refused capture leaves no error behind
+  }
+  cudaEventRecord(M->e0, st);
+  if (M->graph) {
+    if (cudaGraphLaunch(M->graph, st) != cudaSuccess) return DPG_ERR_CUDA;
+  } else if (enqueue_train(M, nf, B, st) != cudaSuccess) {
+    return DPG_ERR_CUDA;
   }
   cudaEventRecord(M->e1, st);
   float hl = 0;
@@ -453,7 +508,7 @@ int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *no
   cudaEventElapsedTime(&ms, M->e0, M->e1);
   M->last_ms = ms;
   // forward + the two backward GEMMs per layer
-  M->last_flops = 3.0 * forward_flops(Bp);
+  M->last_flops = 3.0 * forward_flops(pad128(B));
   return check_err(M);
 }
 

@@ -104,9 +104,12 @@ __device__ __forceinline__ float sigmoid(float x) { return 1.f / (1.f + __expf(-
 
 // loss = mean_b [softplus(l) - y l  +  0.5 w (c - t)^2]; dY (bf16, B x 64,
 // columns >= 2 zero) = d loss / d [l, c]; loss accumulated into *loss_sum
-static __global__ void mlp_loss(const float *out, const float *target, int64_t B, int64_t B_pad, float ctg_weight,
+// (ctg_weight = hp[1]: the step's hyper-parameters live in device memory so a
+// captured training step can be replayed with new values)
+static __global__ void mlp_loss(const float *out, const float *target, int64_t B, int64_t B_pad, const float *hp,
                          __nv_bfloat16 *dY, float *loss_sum) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const float ctg_weight = hp[1];
   float l = 0.f;
   if (b < B_pad) {
     __align__(16) __nv_bfloat16 row[64];
@@ -197,12 +200,12 @@ static __global__ void column_sums_bf16(const __nv_bfloat16 *in, int64_t B, int 
 }
 
 // Adam on FP32 master weights; writes the bf16 copy (and, if wT, its
-// transpose of a rows x cols matrix)
-static __global__ void adam_update(float *w, const float *g, float *m, float *v, int64_t n, float lr, float b1, float b2,
-                            float eps, float bc1, float bc2, __nv_bfloat16 *w16, __nv_bfloat16 *wT, int rows,
-                            int cols) {
+// transpose of a rows x cols matrix).  hp = [lr, ctg_weight, 1 - b1^t, 1 - b2^t]
+static __global__ void adam_update(float *w, const float *g, float *m, float *v, int64_t n, const float *hp, float b1,
+                            float b2, float eps, __nv_bfloat16 *w16, __nv_bfloat16 *wT, int rows, int cols) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const float lr = hp[0], bc1 = hp[2], bc2 = hp[3];
   const float gi = g[i];
   const float mi = b1 * m[i] + (1.f - b1) * gi;
   const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
