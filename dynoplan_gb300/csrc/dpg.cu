@@ -243,7 +243,8 @@ void dpg_destroy(dpg_ctx *c) {
                     &c->x64, &c->nkey32, &c->noff32, &c->mask, &c->cnt, &c->tot, &c->pbase,
                     &c->ord_pbase, &c->ord_ibase, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
                     &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32,
-                    &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill};
+                    &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill,
+                    &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_fill, &c->x64s};
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
@@ -491,6 +492,15 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       (rc = ensure(c, c->ord_pbase, sizeof(unsigned long long) * (P + 1))) ||
       (rc = ensure(c, c->ord_ibase, sizeof(unsigned long long) * (P + 1))))
     return rc;
+  // batches of at least kReorderMin nodes are processed in spatial order
+  const bool reorder = N >= kReorderMin;
+  if (reorder &&
+      ((rc = ensure(c, c->ord_cell, sizeof(uint32_t) * N)) || (rc = ensure(c, c->ord_perm, sizeof(uint32_t) * N)) ||
+       (rc = ensure(c, c->ord_cnt, sizeof(uint32_t) * kOrderCells)) ||
+       (rc = ensure(c, c->ord_start, sizeof(uint32_t) * kOrderCells)) ||
+       (rc = ensure(c, c->ord_fill, sizeof(uint32_t) * kOrderCells)) ||
+       (rc = ensure(c, c->x64s, sizeof(double) * nx * N))))
+    return rc;
   // pair arrays: the caller's device arrays when given, else the arena
   const bool dev_out = opts->out_on_device != 0;
   const size_t capz = (size_t)std::max<int64_t>(cap, 1);
@@ -584,6 +594,22 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   with_kind(kind, [&](auto K) {
     constexpr int KIND = decltype(K)::value;
     using R = Robot<KIND>;
+    if (reorder) {  // nodes by Z-order cell, then index; the pipeline runs on the sorted copy
+      const unsigned nb = (unsigned)((N + 255) / 256);
+      cudaMemsetAsync(c->ord_cnt.p, 0, sizeof(uint32_t) * kOrderCells, st);
+      cudaMemsetAsync(c->ord_fill.p, 0, sizeof(uint32_t) * kOrderCells, st);
+      node_cells<KIND><<<nb, 256, 0, st>>>(P_<double>(c->x64), N, ev, P_<uint32_t>(c->ord_cell),
+                                           P_<uint32_t>(c->ord_cnt));
+      cell_scan<<<1, 1024, 0, st>>>(kOrderCells, P_<uint32_t>(c->ord_cnt), P_<uint32_t>(c->ord_start));
+      cell_scatter<<<nb, 256, 0, st>>>(N, P_<uint32_t>(c->ord_cell), P_<uint32_t>(c->ord_start),
+                                       P_<uint32_t>(c->ord_fill), P_<uint32_t>(c->ord_perm));
+      cell_sort<<<kOrderCells * 32 / 256, 256, 0, st>>>(kOrderCells, P_<uint32_t>(c->ord_start),
+                                                        P_<uint32_t>(c->ord_cnt), P_<uint32_t>(c->ord_perm));
+      gather_nodes<R::NX><<<(unsigned)((N * R::NX + 255) / 256), 256, 0, st>>>(
+          P_<double>(c->x64), P_<uint32_t>(c->ord_perm), N, P_<double>(c->x64s));
+      nv.x64 = P_<double>(c->x64s);
+      ca.nv = nv;
+    }
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
       const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
@@ -606,6 +632,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     cudaEventRecord(c->ev[2], st);
     // exact check: persistent grid, obstacles in shared memory
     if (!(opts->mode & DPG_MODE_BALL_ONLY)) launch_check<KIND>(c, ca, fp64, st);  // ball-only: pairs, no check
+    if (reorder && cap > 0)
+      unpermute_nodes<<<(unsigned)((cap + 255) / 256), 256, 0, st>>>(ctr, cap, P_<uint32_t>(c->ord_perm),
+                                                                    pv_out.node);
     cudaEventRecord(c->ev[3], st);
     cudaEventRecord(c->ev[4], st);
     launch_err = cudaGetLastError();

@@ -6,7 +6,9 @@
 //                   prim) counts; FP64 re-test of |d - r| <= ball_band
 //   nn_prefix       per-primitive exclusive prefix over node tiles
 //   scan_totals     per-primitive bases in length order, work-item bases
-//   nn_emit         pair lists grouped by primitive, nodes ascending
+//   (node_cells, cell_scan, cell_scatter, cell_sort, gather_nodes: batches
+//    of >= kReorderMin nodes are processed in spatial order)
+//   nn_emit         pair lists grouped by primitive, nodes in processing order
 //   check_pairs     persistent warps over (primitive, 32 nodes) work items
 //                   (check_kernels.cuh)
 //
@@ -127,6 +129,117 @@ __global__ void prep_nodes(NodeView nv) {
   for (int i = 0; i < R::POSD; i++) nv.off32[i * nv.N + n] = (float)x[i];
 #pragma unroll
   for (int i = 0; i < R::VELOFF; i++) nv.off32[(R::POSD + i) * nv.N + n] = (float)x[R::vel_comp(i)];
+}
+
+// ------------------------------------------------- spatial order of nodes ---
+// The exact check walks 32 nodes of one primitive per warp; nodes that are
+// close in space see the same obstacles and collide at similar steps, so the
+// batch is processed in Z-order of a 64 x 64 (2-D) or 16^3 (3-D) cell grid
+// over the environment, nodes of a cell by ascending index (deterministic).
+constexpr int kOrderCells = 4096;
+constexpr int64_t kReorderMin = 2048;  // smaller batches keep the caller's order
+
+template <int KIND>
+__global__ void node_cells(const double *x64, int64_t N, EnvView ev, uint32_t *cell, uint32_t *cnt) {
+  using R = Robot<KIND>;
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  constexpr int bits = R::POSD == 3 ? 4 : 6;
+  uint32_t code = 0;
+#pragma unroll
+  for (int d = 0; d < R::POSD; d++) {
+    const double ext = ev.hi[d] - ev.lo[d];
+    double u = ext > 0 ? (x64[n * R::NX + d] - ev.lo[d]) / ext : 0.0;
+    u = u != u ? 0.0 : fmin(fmax(u, 0.0), 1.0);  // NaN / outside: clamp
+    const uint32_t q = min((uint32_t)(u * (1 << bits)), (uint32_t)((1 << bits) - 1));
+#pragma unroll
+    for (int b = 0; b < bits; b++) code |= ((q >> b) & 1u) << (R::POSD * b + d);
+  }
+  cell[n] = code;
+  atomicAdd(&cnt[code], 1u);
+}
+
+// single block: start = exclusive prefix of cnt over n cells
+static __global__ void __launch_bounds__(1024) cell_scan(int n, const uint32_t *cnt, uint32_t *start) {
+  __shared__ uint32_t part[1024];
+  const int t = threadIdx.x, per = (n + 1023) / 1024;
+  const int b = min(n, t * per), e = min(n, b + per);
+  uint32_t sum = 0;
+  for (int i = b; i < e; i++) sum += cnt[i];
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const uint32_t v = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - sum;
+  for (int i = b; i < e; i++) {
+    start[i] = run;
+    run += cnt[i];
+  }
+}
+
+static __global__ void cell_scatter(int64_t N, const uint32_t *cell, const uint32_t *start, uint32_t *fill,
+                                    uint32_t *perm) {
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const uint32_t c = cell[n];
+  perm[start[c] + atomicAdd(&fill[c], 1u)] = (uint32_t)n;
+}
+
+// warp per cell: its nodes by ascending index, which makes the order
+// independent of the scatter's atomics.  Up to 128 nodes: rank sort in
+// registers (node indices are distinct); larger cells: one lane, insertion.
+static __global__ void cell_sort(int n_cells, const uint32_t *start, const uint32_t *cnt, uint32_t *perm) {
+  const int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (c >= n_cells) return;
+  uint32_t *p = perm + start[c];
+  const uint32_t m = cnt[c];
+  if (m <= 1) return;
+  if (m <= 128) {
+    uint32_t v[4], rank[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int r = 0; r < 4; r++) v[r] = (uint32_t)(lane + 32 * r) < m ? p[lane + 32 * r] : 0xffffffffu;
+#pragma unroll
+    for (int rr = 0; rr < 4; rr++) {
+      if ((uint32_t)(32 * rr) >= m) break;
+      for (int l = 0; l < 32; l++) {
+        const uint32_t w = __shfl_sync(kFull, v[rr], l);
+#pragma unroll
+        for (int r = 0; r < 4; r++) rank[r] += (w < v[r]) ? 1u : 0u;
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+      if ((uint32_t)(lane + 32 * r) < m) p[rank[r]] = v[r];
+    return;
+  }
+  if (lane == 0)
+    for (uint32_t i = 1; i < m; i++) {
+      const uint32_t v = p[i];
+      uint32_t j = i;
+      for (; j > 0 && p[j - 1] > v; j--) p[j] = p[j - 1];
+      p[j] = v;
+    }
+}
+
+template <int NX>
+__global__ void gather_nodes(const double *in, const uint32_t *perm, int64_t N, double *out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= N * NX) return;
+  const int64_t n = i / NX;
+  out[i] = in[(int64_t)perm[n] * NX + (i - n * NX)];
+}
+
+// pair lists back to the caller's node numbering (the pairs the emit step
+// wrote: none when the list overflowed the capacity)
+static __global__ void unpermute_nodes(const DevCounters *ctr, int64_t cap, const uint32_t *perm, uint32_t *node) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t n = ctr->n_overflow ? 0 : min((int64_t)ctr->n_pairs, cap);
+  if (i < n) node[i] = perm[node[i]];
 }
 
 // ------------------------------------------------------------ ball scan ---

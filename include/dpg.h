@@ -110,8 +110,12 @@ typedef struct dpg_expand_opts {
 } dpg_expand_opts;
 
 /* Results, one row per in-ball (node, primitive) pair.  Rows are grouped by
- * primitive, primitives in order of decreasing length, nodes ascending
- * within a primitive.  Any array pointer may be NULL to skip that output. */
+ * primitive, primitives in order of decreasing length.  Within a primitive,
+ * nodes come in processing order: ascending index for batches under 2048
+ * nodes, else in Z-order of a coarse grid over the environment (64 x 64
+ * cells, 16^3 in 3-D), ascending index within a cell -- deterministic, and
+ * each node's motions still come in primitive order.  Any array pointer may
+ * be NULL to skip that output. */
 typedef struct dpg_expand_out {
   int64_t capacity;        /* in: rows available in the arrays below */
   int64_t n_pairs;         /* out: rows produced (or needed, on DPG_ERR_CAPACITY) */

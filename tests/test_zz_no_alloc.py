@@ -78,7 +78,11 @@ def test_noalloc_matches_expand_twice(dpg_lib, cfg, scale, precision):
             got["prim"] = got["prim"].view(np.uint32)
             got["n_pairs"] = n
             compare(wl.robot.kind, got, ref, precision)
-            np.testing.assert_array_equal(got["flags"], ref["flags"])
+            # same pairs, possibly in another order within a primitive (large
+            # batches of the regular entry point run in spatial order)
+            kg = np.lexsort((got["node"], got["prim"]))
+            kr = np.lexsort((ref["node"], ref["prim"]))
+            np.testing.assert_array_equal(got["flags"][kg], ref["flags"][kr])
         torch.cuda.synchronize()
         assert torch.cuda.mem_get_info()[0] == free_before   # nothing was allocated
 
