@@ -38,13 +38,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "checked (node,primitive) expansions/s"
 UNIT = "pairs/s"
-KERNELS_PER_STEP = 6  # prep_nodes nn_mask nn_prefix scan_totals nn_emit check_pairs
+# node_cells cell_scan cell_scatter cell_sort gather_nodes (spatial order, batches of
+# >= 2048 nodes) prep_nodes nn_mask nn_prefix scan_totals nn_emit check_pairs unpermute_nodes
+KERNELS_PER_STEP = 12
 L2_FLUSH_BYTES = 512 << 20
 
 # DRAM bytes per check_pairs launch from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum), scaled to the full workload by checked pairs; None
 # until a capture exists.
-CHECK_TRAFFIC_PER_PAIR = 79.8e6 / 4126228  # ncu capture of check_pairs, car1_v0 with 50,000 nodes
+CHECK_TRAFFIC_PER_PAIR = 79.45e6 / 4126228  # ncu capture of check_pairs, car1_v0 with 50,000 nodes
 
 
 def parse():

@@ -104,6 +104,14 @@ SIGNATURES = [
                                             C.c_int32, C.c_int32]),
     ("dpg_primitives_prepare", C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
                                          C.c_uint64]),
+    # include/dpg_roadmap.h
+    ("dpg_roadmap_build", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_double, C.c_double,
+                                    C.POINTER(C.c_void_p)]),
+    ("dpg_roadmap_destroy", None, [C.c_void_p]),
+    ("dpg_roadmap_edges", C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_int64]),
+    ("dpg_roadmap_distances", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("dpg_roadmap_heuristic", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    ("dpg_states_valid", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     # include/dpg_bench.h
     ("dpg_bench_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("dpg_bench_flush_l2", C.c_int, [C.c_int, C.c_size_t]),

@@ -13,6 +13,7 @@
 #include "ctx.h"
 #include "dpg_mlp.h"
 #include "dpg_search.h"
+#include "metric.cuh"
 #include "mlp_kernels.cuh"
 
 using namespace dpg;
@@ -97,52 +98,6 @@ void transformed_state(const dpg_robot_desc &r, const std::vector<double> &st, i
       out[pos[i]] += t * x[vel[i]];
       out[vel[i]] += x[vel[i]];
     }
-  }
-}
-
-// ---- GPU radius query: for each query q, the targets within radius ------
-// (full-state metric, FP32 with an FP64 re-test within `band` of the radius)
-template <int KIND>
-__device__ float full_dist32(const float4 w, const float *a, const float *b) {
-  auto so2f = [](float x, float y) {
-    float d = fabsf(x - y);
-    d = fmodf(d, 6.2831853071795865f);
-    return d > 3.1415926535897932f ? 6.2831853071795865f - d : d;
-  };
-  if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
-    return w.x * hypotf(a[0] - b[0], a[1] - b[1]) + w.y * so2f(a[2], b[2]);
-  } else if constexpr (KIND == DPG_ROBOT_CAR1) {
-    return w.x * hypotf(a[0] - b[0], a[1] - b[1]) + w.y * so2f(a[2], b[2]) + w.z * so2f(a[3], b[3]);
-  } else if constexpr (KIND == DPG_ROBOT_QUAD2D) {
-    return w.x * hypotf(a[0] - b[0], a[1] - b[1]) + w.y * so2f(a[2], b[2]) + w.z * hypotf(a[3] - b[3], a[4] - b[4]) +
-           w.w * fabsf(a[5] - b[5]);
-  } else {
-    float dq = fminf(1.f, fabsf(a[3] * b[3] + a[4] * b[4] + a[5] * b[5] + a[6] * b[6]));
-    auto l3 = [](float x, float y, float z) { return sqrtf(x * x + y * y + z * z); };
-    return w.x * l3(a[0] - b[0], a[1] - b[1], a[2] - b[2]) + w.y * acosf(dq) +
-           w.z * l3(a[7] - b[7], a[8] - b[8], a[9] - b[9]) + w.w * l3(a[10] - b[10], a[11] - b[11], a[12] - b[12]);
-  }
-}
-
-template <int KIND>
-__device__ double full_dist64(const RobotParams &rp, const double *a, const double *b) {
-  auto so2d = [](double x, double y) {
-    double d = fabs(x - y);
-    d = fmod(d, kTwoPi);
-    return d > kPi ? kTwoPi - d : d;
-  };
-  if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
-    return rp.w[0] * hypot(a[0] - b[0], a[1] - b[1]) + rp.w[1] * so2d(a[2], b[2]);
-  } else if constexpr (KIND == DPG_ROBOT_CAR1) {
-    return rp.w[0] * hypot(a[0] - b[0], a[1] - b[1]) + rp.w[1] * so2d(a[2], b[2]) + rp.w[2] * so2d(a[3], b[3]);
-  } else if constexpr (KIND == DPG_ROBOT_QUAD2D) {
-    return rp.w[0] * hypot(a[0] - b[0], a[1] - b[1]) + rp.w[1] * so2d(a[2], b[2]) +
-           rp.w[2] * hypot(a[3] - b[3], a[4] - b[4]) + rp.w[3] * fabs(a[5] - b[5]);
-  } else {
-    double dq = fmin(1.0, fabs(a[3] * b[3] + a[4] * b[4] + a[5] * b[5] + a[6] * b[6]));
-    auto l3 = [](double x, double y, double z) { return sqrt(x * x + y * y + z * z); };
-    return rp.w[0] * l3(a[0] - b[0], a[1] - b[1], a[2] - b[2]) + rp.w[1] * acos(dq) +
-           rp.w[2] * l3(a[7] - b[7], a[8] - b[8], a[9] - b[9]) + rp.w[3] * l3(a[10] - b[10], a[11] - b[11], a[12] - b[12]);
   }
 }
 
@@ -321,6 +276,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   if (!(o->delta > 0) || !(o->alpha > 0 && o->alpha < 1) || o->batch < 1 || o->limit_branching_factor < 1)
     return DPG_ERR_ARG;
   if (o->heuristic == DPG_HEU_MLP && !mlp) return DPG_ERR_ARG;
+  if (o->heuristic == DPG_HEU_ROADMAP && !o->roadmap) return DPG_ERR_ARG;
   std::memset(res, 0, sizeof(*res));
   const auto t_start = std::chrono::steady_clock::now();
   auto elapsed_ms = [&] {
@@ -394,6 +350,11 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   };
   auto heuristic = [&](const double *x) -> float {
     if (o->heuristic == DPG_HEU_BLIND) return 0.f;
+    if (o->heuristic == DPG_HEU_ROADMAP) {
+      double h = 0;
+      dpg_roadmap_heuristic(o->roadmap, 1, x, goal, o->connect_radius_h, &h);
+      return (float)h;
+    }
     return (float)lower_bound_time(r, x, goal);
   };
 
@@ -592,6 +553,12 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       // learned heuristic: the surrogate's cost-to-go of every (node, motion)
       // successor, never below the time lower bound
       std::vector<float> pred;
+      std::vector<double> hroad;  // the roadmap heuristic of every successor of the round
+      if (o->heuristic == DPG_HEU_ROADMAP) {
+        hroad.resize(Q);
+        if ((rc = dpg_roadmap_heuristic(o->roadmap, Q, c_x.data(), goal, o->connect_radius_h, hroad.data())))
+          return rc;
+      }
       if (o->heuristic == DPG_HEU_MLP) {
         const double tm0 = elapsed_ms();
         if (!pnode.reserve(Q) || !pprim.reserve(Q) || !mlp_out.reserve((size_t)Q * 2)) return DPG_ERR_OOM;
@@ -612,6 +579,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
           pos[b]++;
           const double *cx = &c_x[(size_t)ci * nx];
           double h = (o->heuristic == DPG_HEU_BLIND) ? 0.0 : lower_bound_time(r, cx, goal);
+          if (o->heuristic == DPG_HEU_ROADMAP) h = hroad[ci];
           if (o->heuristic == DPG_HEU_MLP) h = std::max(h, kCtgScale * std::max(0.0, (double)pred[2 * (size_t)ci + 1]));
           const double g = (double)nodes[parent].g + c_cost[ci] +
                            o->cost_delta_factor * lower_bound_time(r, &xs[(size_t)parent * nx], &c_x0[(size_t)ci * nx]);

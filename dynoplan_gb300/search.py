@@ -8,7 +8,7 @@ import numpy as np
 from . import _lib
 from ._lib import check
 
-HEU_BLIND, HEU_EUCLIDEAN, HEU_MLP = -1, 0, 1
+HEU_BLIND, HEU_EUCLIDEAN, HEU_MLP, HEU_ROADMAP = -1, 0, 1, 2
 STATUS = {0: "SOLVED", 1: "MAX_EXPANDS", 2: "EMPTY_QUEUE", 3: "MAX_TIME"}
 
 
@@ -17,7 +17,7 @@ class SearchOpts(C.Structure):
                 ("cost_delta_factor", C.c_double), ("limit_branching_factor", C.c_int32), ("batch", C.c_int32),
                 ("max_expands", C.c_int64), ("time_limit_ms", C.c_double), ("heuristic", C.c_int32),
                 ("precision", C.c_int32), ("shuffle", C.c_int32), ("max_neighbors", C.c_int32),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("roadmap", C.c_void_p), ("connect_radius_h", C.c_double)]
 
 
 class SearchResult(C.Structure):
@@ -29,9 +29,11 @@ class SearchResult(C.Structure):
 
 def options(delta, alpha=0.5, batch=1, heuristic=HEU_EUCLIDEAN, limit_branching_factor=20,
             max_expands=100000, time_limit_ms=60000.0, precision=0, shuffle=0, seed=0, max_neighbors=64,
-            delta_factor_goal=1.0, cost_delta_factor=1.0) -> SearchOpts:
+            delta_factor_goal=1.0, cost_delta_factor=1.0, roadmap=None, connect_radius_h=0.5) -> SearchOpts:
+    """roadmap: a dynoplan_gb300.roadmap.Roadmap for HEU_ROADMAP"""
     return SearchOpts(delta, alpha, delta_factor_goal, cost_delta_factor, limit_branching_factor, batch,
-                      max_expands, time_limit_ms, heuristic, precision, shuffle, max_neighbors, seed)
+                      max_expands, time_limit_ms, heuristic, precision, shuffle, max_neighbors, seed,
+                      roadmap.h if roadmap is not None else None, connect_radius_h)
 
 
 def search(ctx, start, goal, opts: SearchOpts, mlp=None, max_path=4096):

@@ -30,6 +30,7 @@
 
 #include "dpg.h"
 #include "dpg_mlp.h"
+#include "dpg_roadmap.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -39,6 +40,7 @@ extern "C" {
 #define DPG_HEU_BLIND -1     /* Heu_blind: 0 */
 #define DPG_HEU_EUCLIDEAN 0  /* Heu_euclidean: lower_bound_time(x, goal) */
 #define DPG_HEU_MLP 1        /* the surrogate's cost-to-go of the (parent, motion) pair */
+#define DPG_HEU_ROADMAP 2    /* Heu_roadmap (reference option 1): include/dpg_roadmap.h */
 
 /* termination (Terminate_status, dbastar.hpp:109-117) */
 #define DPG_SEARCH_SOLVED 0
@@ -63,6 +65,8 @@ typedef struct dpg_search_opts {
   int32_t max_neighbors;          /* unused (kept for layout): neighbour lists are complete,
                                      counted then packed on the GPU */
   uint64_t seed;
+  const struct dpg_roadmap *roadmap; /* DPG_HEU_ROADMAP: a roadmap built for this goal */
+  double connect_radius_h;           /* its query radius (Options_dbastar::connect_radius_h, 0.5) */
 } dpg_search_opts;
 
 typedef struct dpg_search_result {

@@ -201,3 +201,16 @@ def sort_pairs(res, nx):
     for k, v in res.items():
         out[k] = v[order] if isinstance(v, np.ndarray) and len(v) == len(order) else v
     return out
+
+
+def state_valid(model, env, x):
+    """inside the bounds and separated (gap > 0) from every obstacle"""
+    L = lib()
+    L.orc_is_state_valid.argtypes = [C.POINTER(OrcRobot), C.POINTER(OrcEnv), C.c_void_p]
+    L.orc_is_state_valid.restype = C.c_int
+    r = robot(model)
+    e, ke = env_struct(env)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    if not L.orc_is_state_valid(C.byref(r), C.byref(e), _p(x)):
+        return False
+    return all(L.orc_state_gap(C.byref(r), C.byref(e), _p(x), o) > 0.0 for o in range(e.n_obs))

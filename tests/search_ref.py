@@ -69,12 +69,14 @@ def canonical_table(m, prims):
 
 
 def search(m, prims, env, start, goal, delta, alpha=0.5, batch=1, limit=20, max_expands=100000,
-           heuristic=0, dfg=1.0, cdf=1.0):
+           heuristic=0, dfg=1.0, cdf=1.0, hfun=None):
+    """heuristic 0: time lower bound to the goal, -1: blind; hfun(x), when
+    given, replaces both (the roadmap heuristic's restatement)"""
     table = canonical_table(m, prims)
     f32 = np.float32
     X = [np.asarray(start, float)]
     g, h, f, parent, motion, inter, version, in_open = [f32(0)], [], [], [-1], [-1], [-1], [0], [True]
-    h0 = f32(lbt(m, start, goal)) if heuristic == 0 else f32(0)
+    h0 = f32(hfun(start)) if hfun else (f32(lbt(m, start, goal)) if heuristic == 0 else f32(0))
     h.append(h0)
     f.append(f32(g[0] + h0))
     heap = [(f[0], -g[0], 0, 0)]
@@ -138,7 +140,7 @@ def search(m, prims, env, start, goal, delta, alpha=0.5, batch=1, limit=20, max_
                     continue
                 for (cb, p, xe, x0, chosen, cost) in per[b][pos[b]:pos[b] + chunk[b]]:
                     pos[b] += 1
-                    hh = f32(lbt(m, xe, goal)) if heuristic == 0 else f32(0)
+                    hh = f32(hfun(xe)) if hfun else (f32(lbt(m, xe, goal)) if heuristic == 0 else f32(0))
                     gg = float(g[parent_i]) + cost + cdf * float(lbt(m, X[parent_i], x0))
                     nbr = sorted(np.flatnonzero(distance(m, np.array(X), xe[None, :]) <= nov))
                     if not nbr or chosen != -1:
