@@ -112,6 +112,9 @@ SIGNATURES = [
     ("dpg_roadmap_distances", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("dpg_roadmap_heuristic", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
     ("dpg_states_valid", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    # include/dpg_tdb.h
+    ("dpg_tdb_check_pairs", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     # include/dpg_bench.h
     ("dpg_bench_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("dpg_bench_flush_l2", C.c_int, [C.c_int, C.c_size_t]),

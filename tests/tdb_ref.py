@@ -1,0 +1,65 @@
+"""Python restatement of tdb-A*'s check_lazy_trajectory
+(src/tdbastar/tdbastar.cpp:314-447, LazyTraj::compute tdbastar.hpp:172-214)
+over the oracle's bounds and separating-axis gap -- the checker of
+include/dpg_tdb.h, for the translation robots."""
+import math
+
+import numpy as np
+
+import oracle_bind as ob
+
+
+def _states(m, prims, p, x, reverse):
+    xs, _ = prims.motion(p)
+    out = np.array(xs, float)
+    if reverse:
+        out[:, :2] += x[:2] - xs[-1, :2]
+    else:
+        out[:, :2] += x[:2]
+    return out
+
+
+def _in_bounds(env, s):
+    return all(env.lo[i] <= s[i] <= env.hi[i] for i in range(env.dim))
+
+
+def _collides(m, env, s):
+    import ctypes as C
+    L = ob.lib()
+    r = ob.robot(m)
+    e, ke = ob.env_struct(env)
+    s = np.ascontiguousarray(s, dtype=np.float64)
+    return any(L.orc_state_gap(C.byref(r), C.byref(e), s.ctypes.data, o) <= 0.0 for o in range(e.n_obs))
+
+
+def check(m, prims, env, x, node_g, node, prim, reverse, c_time, c_state, goal, delta):
+    out = []
+    for n, p in zip(node, prim):
+        st = _states(m, prims, int(p), x[n], reverse)
+        L = len(st)
+        oob = next((k for k in range(L) if not _in_bounds(env, st[k])), L)
+        if oob < L:
+            out.append((2, oob))
+            continue
+        col = next((k for k in range(L) if _collides(m, env, st[k])), L)
+        if col < L:
+            out.append((1, col))
+            continue
+        v, fi = 0, L
+        if len(c_time):
+            reaches = ob.distance(m, st[L - 1] if reverse else st[0], goal) <= delta
+            g = np.float32(node_g[n])
+            for c, (t, cs) in enumerate(zip(c_time, c_state)):
+                t_off = np.float32(np.float32(t) - g)
+                idx = int(math.floor(float(t_off) / m.dt + 0.5)) if float(t_off) / m.dt >= 0 else \
+                    -int(math.floor(-float(t_off) / m.dt + 0.5))
+                k = -1
+                if reaches and idx >= L - 1:
+                    k = L - 1
+                if 0 <= idx < L - 1:
+                    k = idx
+                if k >= 0 and ob.distance(m, st[k], cs) <= delta:
+                    v, fi = 3, c
+                    break
+        out.append((v, fi))
+    return np.array(out, np.int64).reshape(-1, 2)

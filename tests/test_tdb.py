@@ -1,0 +1,76 @@
+"""tdb-A*'s pair checks (include/dpg_tdb.h): forward and reverse verdicts
+and the constraint test against tests/tdb_ref.py; the forward transform of
+the rollout robots against the regular FP64 check."""
+import numpy as np
+import pytest
+
+from dynoplan_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("cfg,reverse", [(1, False), (1, True), (2, False), (2, True)])
+def test_tdb_checks_match_restatement(dpg_lib, cfg, reverse):
+    import tdb_ref
+    from dynoplan_gb300 import gpu as G
+    from dynoplan_gb300 import tdb as T
+    wl = W.make_workload(cfg, scale=0.02, seed=40 + cfg)
+    m = wl.robot
+    rng = np.random.default_rng(cfg + 10 * reverse)
+    N = len(wl.nodes)
+    n = 3000
+    node = rng.integers(0, N, n)
+    prim = rng.integers(0, wl.prims.P, n)
+    node_g = rng.uniform(0, 5, N).astype(np.float32)
+    goal = wl.nodes[0]
+    delta = 0.3
+    with G.Context(m) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        v0, fi0, _ = T.check_pairs(ctx, wl.nodes, node, prim, reverse=reverse)
+        # constraints taken from states of valid pairs, so that some pairs violate them
+        valid = np.flatnonzero(v0 == 0)
+        assert len(valid) > 20
+        pick = rng.choice(valid, 12, replace=False)
+        c_time, c_state = [], []
+        for i in pick:
+            st = tdb_ref._states(m, wl.prims, int(prim[i]), wl.nodes[node[i]], reverse)
+            k = int(rng.integers(0, len(st)))
+            c_time.append(float(node_g[node[i]]) + k * m.dt + float(rng.uniform(-0.02, 0.02)))
+            c_state.append(st[k] + rng.normal(0, 0.05, m.nx))
+        c_time, c_state = np.array(c_time), np.array(c_state)
+        v, fi, end = T.check_pairs(ctx, wl.nodes, node, prim, reverse=reverse, node_g=node_g, c_time=c_time,
+                                   c_state=c_state, goal=goal, delta=delta)
+    ref = tdb_ref.check(m, wl.prims, wl.env, wl.nodes, node_g, node, prim, reverse, c_time, c_state, goal, delta)
+    assert np.array_equal(v.astype(np.int64), ref[:, 0])
+    assert np.array_equal(fi.astype(np.int64), ref[:, 1])
+    assert (v == T.CONSTRAINT_VIOLATION).sum() >= 12
+    assert np.array_equal(v0[v != T.CONSTRAINT_VIOLATION], v[v != T.CONSTRAINT_VIOLATION])
+
+
+@pytest.mark.parametrize("cfg", [3, 5])
+def test_tdb_forward_rollout_robots_match_check_pairs(dpg_lib, cfg):
+    from dynoplan_gb300 import gpu as G
+    from dynoplan_gb300 import tdb as T
+    wl = W.make_workload(cfg, scale=0.01, seed=60 + cfg)
+    with G.Context(wl.robot) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        r = ctx.expand(wl.nodes, wl.radius, precision=1)
+        v, fi, end = T.check_pairs(ctx, wl.nodes, r["node"], r["prim"])
+    assert r["n_pairs"] > 0
+    assert np.array_equal(v, r["verdict"])
+    assert np.array_equal(fi, r["first_invalid"].astype(np.int32))
+    assert np.allclose(end, r["end_state"], rtol=0, atol=1e-9)
+
+
+def test_tdb_rejects_reverse_for_rollout_robots(dpg_lib):
+    from dynoplan_gb300 import gpu as G
+    from dynoplan_gb300 import tdb as T
+    from dynoplan_gb300._lib import DpgError
+    wl = W.make_workload(5, scale=0.005)
+    with G.Context(wl.robot) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        with pytest.raises(DpgError):
+            T.check_pairs(ctx, wl.nodes, [0], [0], reverse=True)
