@@ -143,6 +143,54 @@ static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
   return (ntiles + y - 1) / y;
 }
 
+// Ball scan of the nv.N nodes against the pv.P primitives: bitmask words
+// (W x Ppad), per-tile counts cnt[B][P] turned into prefixes, totals tot[P].
+// Batches of at least kGridMin nodes of a robot with a key grid test only the
+// primitives of the cells near their key; smaller batches test every
+// primitive (split over the primitives too, to fill the GPU).  Both give the
+// same mask and counts.
+constexpr int64_t kGridMin = 2048;
+template <int KIND>
+static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv, double radius, double ball_band,
+                        int Ppad, int64_t B, int64_t W, uint32_t *mask, uint32_t *cnt, uint32_t *tot,
+                        DevCounters *ctr, cudaStream_t st) {
+  using R = Robot<KIND>;
+  const RobotParams &rp = c->rp;
+  const int P = pv.P;
+  const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
+  bool done = false;
+  if constexpr (R::KEYD <= 2) {
+    if (c->kg.n0 > 0 && nv.N >= kGridMin) {
+      // half-width of the cell range along a key component: radius plus band
+      // over its weight, widened; -1 = every cell
+      auto half = [&](double wk, bool periodic) -> float {
+        const double h = (radius + ball_band) / wk * (1.0 + 1e-4) + 1e-3;
+        if (!(wk > 0) || !std::isfinite(h) || (periodic && h >= kPi)) return -1.f;
+        return (float)h;
+      };
+      const float h0 = half(rp.w[1], true);
+      const float h1 = half(KIND == DPG_ROBOT_CAR1 ? rp.w[2] : rp.w[3], KIND == DPG_ROBOT_CAR1);
+      cudaMemsetAsync(mask, 0, sizeof(uint32_t) * (size_t)W * Ppad, st);
+      if (P <= kGridSmemP) {
+        nn_grid<KIND, true><<<(unsigned)B, kNNThreads, sizeof(uint32_t) * P, st>>>(
+            rp, pv, nv, c->kg, w32, (float)radius, radius, (float)ball_band, h0, h1, Ppad, mask, cnt, ctr);
+      } else {
+        cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (size_t)B * P, st);
+        nn_grid<KIND, false><<<(unsigned)B, kNNThreads, 0, st>>>(rp, pv, nv, c->kg, w32, (float)radius, radius,
+                                                                 (float)ball_band, h0, h1, Ppad, mask, cnt, ctr);
+      }
+      done = true;
+    }
+  }
+  if (!done) {
+    const int tpy = nn_tiles_per_y(P, B, c->sm_count);
+    const dim3 ng((unsigned)B, (unsigned)((P + tpy * kNNTile - 1) / (tpy * kNNTile)));
+    nn_mask<KIND><<<ng, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)radius, radius, (float)ball_band, Ppad, tpy,
+                                             mask, cnt, ctr);
+  }
+  nn_prefix<<<(unsigned)((P + 31) / 32), 256, 0, st>>>(P, (int)B, cnt, tot);
+}
+
 extern "C" {
 
 int dpg_abi_version(void) { return DPG_ABI_VERSION; }
@@ -244,7 +292,8 @@ void dpg_destroy(dpg_ctx *c) {
                     &c->ord_pbase, &c->ord_ibase, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
                     &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32,
                     &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill,
-                    &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_fill, &c->x64s};
+                    &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_fill, &c->x64s,
+                    &c->kg_start, &c->kg_tab};
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
@@ -261,6 +310,76 @@ const char *dpg_last_error(const dpg_ctx *c) { return c ? c->err.c_str() : "null
 
 // Host index, raw device tables and every derived table of a primitive set.
 // `states` / `actions` are host arrays (H2D) or device arrays (D2D, `kind`).
+// Key-space grid of the primitives for robots with one or two key
+// components: about two primitives per cell, primitives listed by cell in
+// id order.  Built from the device key table the ball scan reads, so a
+// primitive's cell is that of the key it is tested with.
+static int build_key_grid(dpg_ctx *c, int P) {
+  const int kind = c->robot.kind, kd = key_dim(kind);
+  c->kg = KeyGrid{};
+  if (kd > 2) return DPG_OK;
+  std::vector<float> key((size_t)kd * P), kc(P);
+  CUDA_TRY(c, cudaMemcpy(key.data(), c->key32.p, sizeof(float) * kd * P, cudaMemcpyDeviceToHost));
+  CUDA_TRY(c, cudaMemcpy(kc.data(), c->kconst32.p, sizeof(float) * P, cudaMemcpyDeviceToHost));
+  KeyGrid g{};
+  if (kd == 1) {
+    g.n0 = std::clamp(P / 2, 1, 4096);
+    g.n1 = 1;
+  } else {
+    g.n0 = g.n1 = std::clamp((int)std::lround(std::sqrt(P / 2.0)), 1, 128);
+  }
+  const bool per1 = kind == DPG_ROBOT_CAR1;
+  g.inv0 = (float)(g.n0 / kTwoPi);
+  if (kd > 1 && per1) {
+    g.inv1 = (float)(g.n1 / kTwoPi);
+  } else if (kd > 1) {
+    float lo = 0.f, hi = 0.f;
+    bool any = false;
+    for (int p = 0; p < P; p++) {
+      const float k = key[(size_t)P + p];
+      if (!std::isfinite(k)) continue;
+      lo = any ? std::min(lo, k) : k;
+      hi = any ? std::max(hi, k) : k;
+      any = true;
+    }
+    g.lo1 = lo;
+    g.inv1 = hi > lo ? (float)(g.n1 / ((double)hi - lo)) : 0.f;
+  }
+  // same float arithmetic as the query's ranges; NaN keys (never members) in cell 0
+  auto cell = [](float f, int n) { return std::isfinite(f) ? kg_clamp((int)std::max(-1.f, std::min(f, (float)n)), n) : 0; };
+  const float piF = 3.14159265f;
+  const int ncell = g.n0 * g.n1;
+  std::vector<uint32_t> cid(P), start(ncell + 1, 0u);
+  for (int p = 0; p < P; p++) {
+    const int c0 = cell(std::floor((key[p] + piF) * g.inv0), g.n0);
+    int c1 = 0;
+    if (kd > 1) {
+      const float k1 = key[(size_t)P + p];
+      c1 = per1 ? cell(std::floor((k1 + piF) * g.inv1), g.n1) : cell(std::floor((k1 - g.lo1) * g.inv1), g.n1);
+    }
+    cid[p] = (uint32_t)(c0 * g.n1 + c1);
+    start[cid[p] + 1]++;
+  }
+  for (int i = 0; i < ncell; i++) start[i + 1] += start[i];
+  std::vector<float4> tab(P);
+  std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+  for (int p = 0; p < P; p++) {
+    float id;
+    std::memcpy(&id, &p, sizeof id);
+    tab[fill[cid[p]]++] = make_float4(key[p], kd > 1 ? key[(size_t)P + p] : 0.f, kc[p], id);
+  }
+  int rc;
+  if ((rc = ensure(c, c->kg_start, sizeof(uint32_t) * (ncell + 1))) ||
+      (rc = ensure(c, c->kg_tab, sizeof(float4) * P)))
+    return rc;
+  CUDA_TRY(c, cudaMemcpy(c->kg_start.p, start.data(), sizeof(uint32_t) * (ncell + 1), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->kg_tab.p, tab.data(), sizeof(float4) * P, cudaMemcpyHostToDevice));
+  g.start = P_<uint32_t>(c->kg_start);
+  g.tab = P_<float4>(c->kg_tab);
+  c->kg = g;
+  return DPG_OK;
+}
+
 static int load_tables(dpg_ctx *c, int32_t P, const int32_t *len, const double *states, const double *actions,
                        cudaMemcpyKind copy) {
   const int nx = c->robot.nx, nu = c->robot.nu, kind = c->robot.kind;
@@ -330,6 +449,7 @@ static int load_tables(dpg_ctx *c, int32_t P, const int32_t *len, const double *
   });
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaStreamSynchronize(st));
+  if ((rc = build_key_grid(c, P)) != DPG_OK) return rc;
   c->P = P;
   c->S = S;
   c->A = A;
@@ -612,12 +732,8 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     }
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
-      const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
-      const int tpy = nn_tiles_per_y(P, B, c->sm_count);
-      const dim3 ng((unsigned)B, (unsigned)((P + tpy * kNNTile - 1) / (tpy * kNNTile)));
-      nn_mask<KIND><<<ng, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)opts->radius, opts->radius, (float)ball_band,
-                                               Ppad, tpy, P_<uint32_t>(c->mask), P_<uint32_t>(c->cnt), ctr);
-      nn_prefix<<<(P + 255) / 256, 256, 0, st>>>(P, (int)B, P_<uint32_t>(c->cnt), P_<uint32_t>(c->tot));
+      launch_ball<KIND>(c, pv, nv, opts->radius, ball_band, Ppad, B, W, P_<uint32_t>(c->mask),
+                        P_<uint32_t>(c->cnt), P_<uint32_t>(c->tot), ctr, st);
     } else {
       cudaMemsetAsync(c->tot.p, 0, sizeof(uint32_t) * P, st);
     }
@@ -838,12 +954,7 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
     using R = Robot<KIND>;
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
-      const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
-      const int tpy = nn_tiles_per_y(P, B, c->sm_count);
-      const dim3 ng((unsigned)B, (unsigned)((P + tpy * kNNTile - 1) / (tpy * kNNTile)));
-      nn_mask<KIND><<<ng, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)opts->radius, opts->radius, (float)ball_band,
-                                               Ppad, tpy, mask, cnt, ctr);
-      nn_prefix<<<(P + 255) / 256, 256, 0, st>>>(P, (int)B, cnt, tot);
+      launch_ball<KIND>(c, pv, nv, opts->radius, ball_band, Ppad, B, W, mask, cnt, tot, ctr, st);
     } else {
       cudaMemsetAsync(tot, 0, sizeof(uint32_t) * P, st);
     }

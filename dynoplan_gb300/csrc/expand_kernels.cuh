@@ -333,17 +333,127 @@ __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView p
   if (lane == 0 && rechecks) atomicAdd(&ctr->n_ball_recheck, rechecks);
 }
 
-// per primitive: cnt[b][p] -> exclusive prefix over b; tot[p] = total
-static __global__ void nn_prefix(int P, int B, uint32_t *cnt, uint32_t *tot) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
+// Key-space grid of the primitives (robots whose kept key has one or two
+// components): cells over key component 0 (an angle, periodic) and
+// component 1 (an angle for car1, periodic; the angular rate for quad2d,
+// linear over the primitives' range), primitives listed by cell (CSR).
+struct KeyGrid {
+  int n0, n1;              // cells per component (n1 = 1 for one component)
+  float inv0, lo1, inv1;   // cell = floor((k + pi) inv0), floor((k - lo1) inv1)
+  const uint32_t *start;   // [n0 n1 + 1]
+  const float4 *tab;       // [P] (key 0, key 1, constant part, primitive id bits)
+};
+
+__host__ __device__ __forceinline__ int kg_clamp(int c, int n) { return c < 0 ? 0 : (c >= n ? n - 1 : c); }
+
+// Ball membership through the key grid: thread per node, each node tests the
+// primitives of the cells within h0 / h1 (the radius plus the band over the
+// component's weight, widened; negative = the whole range) of its key, with
+// the same FP32 test and FP64 band decision as nn_mask, so the bitmask and
+// the counts are the same.  The mask must be zero on entry; members set
+// their bit with atomicOr.  cnt[b][p] is counted in shared memory when
+// SCNT (P <= kGridSmemP), else by global atomics into a zeroed cnt.
+constexpr int kGridSmemP = 12288;
+template <int KIND, bool SCNT>
+__global__ void __launch_bounds__(kNNThreads) nn_grid(RobotParams rp, PrimView pv, NodeView nv, KeyGrid kg,
+                                                      float4 w32, float radius, double radius64, float band,
+                                                      float h0, float h1, int Ppad, uint32_t *mask, uint32_t *cnt,
+                                                      DevCounters *ctr) {
+  using R = Robot<KIND>;
+  static_assert(R::KEYD <= 2, "key grid: one or two key components");
+  constexpr bool kPer1 = KIND == DPG_ROBOT_CAR1;  // second component an angle
+  constexpr float kPiF = 3.14159265f;
+  extern __shared__ uint32_t scnt[];
+  if (SCNT) {
+    for (int t = threadIdx.x; t < pv.P; t += blockDim.x) scnt[t] = 0;
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (int64_t)blockIdx.x * (kNNThreads / 32) + (threadIdx.x >> 5);
+  const int64_t n = w * 32 + lane;
+  unsigned long long rechecks = 0;
+  if (n < nv.N) {
+    float nk[2];
+    nk[0] = nv.key32[n];
+    nk[1] = R::KEYD > 1 ? nv.key32[nv.N + n] : 0.f;
+    // cell ranges; a NaN key or a range of a whole period takes every cell
+    // (node angles are wrapped to [-pi, pi] and h0 inv0 <= n0, so the
+    // conversions stay small)
+    int a0 = 0, a1 = kg.n0 - 1, b0 = 0, b1 = kg.n1 - 1;
+    if (h0 >= 0.f) {
+      const float f0 = floorf((nk[0] - h0 + kPiF) * kg.inv0), f1 = floorf((nk[0] + h0 + kPiF) * kg.inv0);
+      if (f1 - f0 + 1.f < (float)kg.n0) { a0 = (int)f0; a1 = (int)f1; }
+    }
+    if (R::KEYD > 1 && h1 >= 0.f) {
+      if (kPer1) {
+        const float f0 = floorf((nk[1] - h1 + kPiF) * kg.inv1), f1 = floorf((nk[1] + h1 + kPiF) * kg.inv1);
+        if (f1 - f0 + 1.f < (float)kg.n1) { b0 = (int)f0; b1 = (int)f1; }
+      } else {
+        b0 = kg_clamp((int)floorf(fmaxf((nk[1] - h1 - kg.lo1) * kg.inv1, -1.f)), kg.n1);
+        b1 = kg_clamp((int)floorf(fminf((nk[1] + h1 - kg.lo1) * kg.inv1, (float)kg.n1)), kg.n1);
+      }
+    }
+    const double *xn = nv.x64 + n * R::NX;
+    uint32_t *mrow = mask + w * (int64_t)Ppad;
+    const uint32_t bit = 1u << lane;
+    for (int a = a0; a <= a1; a++) {
+      const int ca = ((a % kg.n0) + kg.n0) % kg.n0;
+      for (int b = b0; b <= b1;) {  // runs of cells contiguous in the row
+        const int cb = kPer1 ? ((b % kg.n1) + kg.n1) % kg.n1 : b;
+        const int last = kPer1 ? min(b1, b + (kg.n1 - 1 - cb)) : b1;
+        const uint32_t s = kg.start[ca * kg.n1 + cb], e = kg.start[ca * kg.n1 + cb + (last - b) + 1];
+        for (uint32_t i = s; i < e; i++) {
+          const float4 t = kg.tab[i];
+          const float sk[2] = {t.x, t.y};
+          const float d = key_dist32<KIND>(w32, nk, sk, 1, t.z);
+          bool in = d <= radius;
+          const int p = __float_as_int(t.w);
+          if (fabsf(d - radius) <= band) {  // decide in FP64
+            in = key_dist64<KIND>(rp, xn, pv.st64 + pv.soff[p] * R::NX) <= radius64;
+            rechecks++;
+          }
+          if (in) {
+            atomicOr(&mrow[p], bit);
+            if (SCNT) atomicAdd(&scnt[p], 1u);
+            else atomicAdd(&cnt[(int64_t)blockIdx.x * pv.P + p], 1u);
+          }
+        }
+        b = last + 1;
+      }
+    }
+  }
+  if (SCNT) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < pv.P; t += blockDim.x) cnt[(int64_t)blockIdx.x * pv.P + t] = scnt[t];
+  }
+  for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_down_sync(kFull, rechecks, o);
+  if (lane == 0 && rechecks) atomicAdd(&ctr->n_ball_recheck, rechecks);
+}
+
+// per primitive: cnt[b][p] -> exclusive prefix over b; tot[p] = total.
+// Block = 32 primitives (lanes) x 8 segments of the node tiles (warps).
+static __global__ void __launch_bounds__(256) nn_prefix(int P, int B, uint32_t *cnt, uint32_t *tot) {
+  __shared__ uint32_t part[8][32];
+  const int pl = threadIdx.x & 31, sg = threadIdx.x >> 5;
+  const int p = blockIdx.x * 32 + pl;
+  const int per = (B + 7) / 8;
+  const int b0 = min(B, sg * per), b1 = min(B, b0 + per);
+  uint32_t s = 0;
+  if (p < P) {
+#pragma unroll 8
+    for (int b = b0; b < b1; b++) s += cnt[(int64_t)b * P + p];
+  }
+  part[sg][pl] = s;
+  __syncthreads();
   uint32_t run = 0;
-  for (int b = 0; b < B; b++) {
+  for (int k = 0; k < sg; k++) run += part[k][pl];
+  if (p >= P) return;
+  for (int b = b0; b < b1; b++) {
     const uint32_t c = cnt[(int64_t)b * P + p];
     cnt[(int64_t)b * P + p] = run;
     run += c;
   }
-  tot[p] = run;
+  if (sg == 7) tot[p] = run;
 }
 
 // Single block: bases of each primitive's pair segment and of its work
@@ -405,10 +515,16 @@ static __global__ void __launch_bounds__(256) nn_emit(int P, int Ppad, int64_t W
   const int64_t b = blockIdx.y;
   if (p >= P) return;
   unsigned long long pos = pbase[p] + loc[b * P + p];
+  uint32_t words[kNNThreads / 32];  // all loads in flight before the walk
+#pragma unroll
   for (int k = 0; k < kNNThreads / 32; k++) {
     const int64_t w = b * (kNNThreads / 32) + k;
-    if (w >= W) break;
-    uint32_t word = mask[w * Ppad + p];
+    words[k] = w < W ? mask[w * Ppad + p] : 0u;
+  }
+#pragma unroll
+  for (int k = 0; k < kNNThreads / 32; k++) {
+    const int64_t w = b * (kNNThreads / 32) + k;
+    uint32_t word = words[k];
     while (word) {
       const int bit = __ffs(word) - 1;
       word &= word - 1;
