@@ -22,7 +22,9 @@
 //      pair; bitmask over <= kMaxCullObs obstacles),
 //   2. against the box of each chunk of kChunk states (from the level-1 set),
 // then every state tests its chunk's candidates (separating axes, AABB early
-// reject).  A test whose FP32 gap lies within `band` of zero, and a bounds
+// reject).  Bounds tests run only in chunks whose box is not inside the
+// bounds, and a chunk in which no lane has an obstacle or bounds test to make
+// is stepped over as a whole.  A test whose FP32 gap lies within `band` of zero, and a bounds
 // test within `band` of a bound, is recomputed in FP64 from the FP64 tables
 // on the spot, so verdicts equal the FP64 oracle's.
 #pragma once
@@ -245,6 +247,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   const Real hw = F32 ? Real(A.half_wid32) : Real(rp.half_wid);
   const Real rad = F32 ? Real(A.radius32) : Real(rp.radius);
   uint32_t cm[kMaxCullObs / 32] = {0u, 0u, 0u, 0u};
+  bool nb = need_bounds;  // bounds tests in the current chunk
 
   for (int k = 0; k < L; k++) {
     if (LOCKSTEP) {
@@ -253,8 +256,9 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
       break;
     }
     const Real t = Real(k) * dtR;
-    // level-2 culling at each chunk start
-    if (CULL && (k % kChunk) == 0 && !done && !collided) {
+    // at each chunk start: the chunk's box (the parts over its kChunk states,
+    // transformed), level-2 culling, and whether its states need bounds tests
+    if (CULL && (k % kChunk) == 0) {
       const float *cb = pv.cbox32 + (pv.coff[p] + k / kChunk) * 2 * D;
       const float t0 = float(k) * A.dt32, t1 = float(min(L - 1, k + kChunk - 1)) * A.dt32;
       float cen[D], hf[D];
@@ -268,15 +272,35 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
           hf[i] += 0.5f * (t1 - t0) * fabsf(v);
         }
       }
+      if (!done && !collided) {
 #pragma unroll
-      for (int w = 0; w < kMaxCullObs / 32; w++) {
-        uint32_t m = l1[w], c = 0;
-        while (m) {
-          const int b = __ffs(m) - 1;
-          m &= m - 1;
-          if (near_box<D, Real>(cen, hf, obs_sm, 32 * w + b, M)) c |= 1u << b;
+        for (int w = 0; w < kMaxCullObs / 32; w++) {
+          uint32_t m = l1[w], c = 0;
+          while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            if (near_box<D, Real>(cen, hf, obs_sm, 32 * w + b, M)) c |= 1u << b;
+          }
+          cm[w] = c;
         }
-        cm[w] = c;
+      }
+      // the box holds every state position of the chunk: inside the bounds
+      // with the band and an arithmetic slack, no state of it is out
+      if (need_bounds) {
+        bool in = true;
+#pragma unroll
+        for (int i = 0; i < D; i++)
+          in = in && cen[i] - hf[i] > A.lo32[i] + A.band32 + 1e-3f && cen[i] + hf[i] < A.hi32[i] - A.band32 - 1e-3f;
+        nb = !in;
+      }
+      // no lane has an obstacle test or a bounds test to make in this chunk:
+      // its states change nothing (no contact, no bound, no min_gap update)
+      if (LOCKSTEP) {
+        const bool idle = done || ((collided || (cm[0] | cm[1] | cm[2] | cm[3]) == 0u) && !nb);
+        if (__all_sync(kFull, idle)) {
+          k += kChunk - 1;
+          continue;
+        }
       }
     }
     if (done) continue;
@@ -287,7 +311,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
     Real sx = off[0], sy = off[1], sz = Real(0);
     if (V) { sx += t * off[D + 0]; sy += t * off[D + 1]; }
     if (D == 3) { sz = off[2]; if (V) sz += t * off[D + 2]; }
-    if (need_bounds) {
+    if (nb) {
       const Real pv3[3] = {ps[0].cx + sx, ps[0].cy + sy, ps[0].c + sz};
       int bt = 0;
 #pragma unroll
