@@ -20,7 +20,7 @@
 // fall in the FP64 band or set min_gap is dropped:
 //   1. against the bounding box of the whole transformed primitive (once per
 //      pair; bitmask over <= kMaxCullObs obstacles),
-//   2. against the box of each chunk of kChunk states (from the level-1 set),
+//   2. against the box of each chunk of R::CHUNK states (from the level-1 set),
 // then every state tests its chunk's candidates (separating axes, AABB early
 // reject).  Bounds tests run only in chunks whose box is not inside the
 // bounds, and a chunk in which no lane has an obstacle or bounds test to make
@@ -256,11 +256,11 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
       break;
     }
     const Real t = Real(k) * dtR;
-    // at each chunk start: the chunk's box (the parts over its kChunk states,
+    // at each chunk start: the chunk's box (the parts over its R::CHUNK states,
     // transformed), level-2 culling, and whether its states need bounds tests
-    if (CULL && (k % kChunk) == 0) {
-      const float *cb = pv.cbox32 + (pv.coff[p] + k / kChunk) * 2 * D;
-      const float t0 = float(k) * A.dt32, t1 = float(min(L - 1, k + kChunk - 1)) * A.dt32;
+    if (CULL && (k % R::CHUNK) == 0) {
+      const float *cb = pv.cbox32 + (pv.coff[p] + k / R::CHUNK) * 2 * D;
+      const float t0 = float(k) * A.dt32, t1 = float(min(L - 1, k + R::CHUNK - 1)) * A.dt32;
       float cen[D], hf[D];
 #pragma unroll
       for (int i = 0; i < D; i++) {
@@ -298,7 +298,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
       if (LOCKSTEP) {
         const bool idle = done || ((collided || (cm[0] | cm[1] | cm[2] | cm[3]) == 0u) && !nb);
         if (__all_sync(kFull, idle)) {
-          k += kChunk - 1;
+          k += R::CHUNK - 1;
           continue;
         }
       }

@@ -388,12 +388,14 @@ static int load_tables(dpg_ctx *c, int32_t P, const int32_t *len, const double *
   c->h_aoff.resize(P);
   c->h_coff.resize(P);
   int64_t S = 0, A = 0, NC = 0;
+  int chunk = 0;
+  with_kind(kind, [&](auto K) { chunk = Robot<decltype(K)::value>::CHUNK; });
   for (int p = 0; p < P; p++) {
     if (len[p] < 1 || len[p] > 32767) return fail(c, DPG_ERR_ARG, "upload_primitives: length out of [1, 32767]");
     c->h_soff[p] = S;
     c->h_aoff[p] = A;
     c->h_coff[p] = NC;
-    NC += (len[p] + kChunk - 1) / kChunk;
+    NC += (len[p] + chunk - 1) / chunk;
     S += len[p];
     A += len[p] - 1;
   }

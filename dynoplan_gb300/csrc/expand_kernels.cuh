@@ -32,7 +32,6 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kNNThreads = 256;   // 8 warps = 8 bitmask words = 256 nodes
 constexpr int kNNTile = 256;      // primitives staged per shared-memory tile
 constexpr int kCheckThreads = 256;
-constexpr int kChunk = 8;          // states per culling chunk
 constexpr int kMaxCullObs = 128;   // per-lane candidate bitmask covers this many obstacles
 constexpr float kGapCap = 0.05f;   // min_gap is exact up to this clearance, +inf above
 
@@ -68,7 +67,7 @@ struct PrimView {
   const float *pbox32;       // the same, rounded outward
   const int64_t *coff;       // [P] first chunk row of primitive p
   const float *cbox32;       // [sum chunks][2*POSD]: centre..., half... of the parts'
-                             //   bounding box over kChunk states (outward rounded)
+                             //   bounding box over Robot::CHUNK states (outward rounded)
   const float *tbox32;       // [P][2*POSD]: the same over the whole primitive
 };
 
@@ -618,7 +617,7 @@ __global__ void build_keys(RobotParams rp, int P, const int32_t *len, const int6
   }
 }
 
-// Culling boxes: per chunk of kChunk states, the bounding box of every
+// Culling boxes: per chunk of Robot::CHUNK states, the bounding box of every
 // collision part over those canonical states; per primitive, the union.
 // FP64, then rounded outward to FP32 (centre to nearest, half extent up by
 // the centre's rounding error).
@@ -632,9 +631,9 @@ __global__ void build_chunks(RobotParams rp, int P, const int32_t *len, const in
   if (p >= P) return;
   double tlo[3] = {1e300, 1e300, 1e300}, thi[3] = {-1e300, -1e300, -1e300};
   const int L = len[p];
-  for (int c = 0; c * kChunk < L; c++) {
+  for (int c = 0; c * R::CHUNK < L; c++) {
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int k = c * kChunk; k < min(L, (c + 1) * kChunk); k++) {
+    for (int k = c * R::CHUNK; k < min(L, (c + 1) * R::CHUNK); k++) {
       for (int q = 0; q < R::PARTS; q++) {
         const Pose<double> ps = pose64[q * S + soff[p] + k];
         if constexpr (R::SPHERE) {

@@ -40,6 +40,7 @@ template <> struct Robot<DPG_ROBOT_UNICYCLE1> {
   static constexpr int NX = 3, NU = 2, PARTS = 1, POSD = 2, VELOFF = 0;
   static constexpr bool ROLLOUT = false, SPHERE = false;
   static constexpr int KEYD = 1;  // kept key components: theta
+  static constexpr int CHUNK = 8;  // states per culling chunk
   __host__ __device__ static int key_comp(int i) { return 2; }
   __host__ __device__ static int vel_comp(int i) { return -1; }
 };
@@ -48,6 +49,7 @@ template <> struct Robot<DPG_ROBOT_CAR1> {
   static constexpr int NX = 4, NU = 2, PARTS = 2, POSD = 2, VELOFF = 0;
   static constexpr bool ROLLOUT = false, SPHERE = false;
   static constexpr int KEYD = 2;  // theta0, theta1
+  static constexpr int CHUNK = 8;
   __host__ __device__ static int key_comp(int i) { return 2 + i; }
   __host__ __device__ static int vel_comp(int i) { return -1; }
 };
@@ -56,6 +58,7 @@ template <> struct Robot<DPG_ROBOT_QUAD2D> {
   static constexpr int NX = 6, NU = 2, PARTS = 1, POSD = 2, VELOFF = 2;
   static constexpr bool ROLLOUT = true, SPHERE = false;
   static constexpr int KEYD = 2;  // theta, w
+  static constexpr int CHUNK = 16;  // dt 0.01: ten times the states of the others per second
   __host__ __device__ static int key_comp(int i) { return i == 0 ? 2 : 5; }
   __host__ __device__ static int vel_comp(int i) { return 3 + i; }
 };
@@ -64,6 +67,7 @@ template <> struct Robot<DPG_ROBOT_QUAD3D> {
   static constexpr int NX = 13, NU = 4, PARTS = 1, POSD = 3, VELOFF = 3;
   static constexpr bool ROLLOUT = true, SPHERE = true;
   static constexpr int KEYD = 7;  // quaternion (4), w (3)
+  static constexpr int CHUNK = 16;
   __host__ __device__ static int key_comp(int i) { return i < 4 ? 3 + i : 6 + i; }
   __host__ __device__ static int vel_comp(int i) { return 7 + i; }
 };
