@@ -427,7 +427,7 @@ __device__ void load_obstacles(const EnvView &ev, void *sm) {
 
 // Persistent warps over (primitive, 32 nodes) work items.
 template <int KIND, class Real, bool BAND, bool CULL>
-__global__ void __launch_bounds__(kCheckThreads, 4) check_pairs(CheckArgs A) {
+__global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) check_pairs(CheckArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   load_obstacles<Real, KIND>(A.ev, smem);
   const int lane = threadIdx.x & 31;
