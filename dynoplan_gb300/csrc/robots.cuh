@@ -41,7 +41,7 @@ template <> struct Robot<DPG_ROBOT_UNICYCLE1> {
   static constexpr bool ROLLOUT = false, SPHERE = false;
   static constexpr int KEYD = 1;  // kept key components: theta
   static constexpr int CHUNK = 8;  // states per culling chunk
-  static constexpr int CHECK_BLOCKS = 4;  // check_pairs blocks per SM (register bound; measured: 4 beats 3, 5 and 6 for car1)
+  static constexpr int CHECK_BLOCKS = 4;  // check_pairs blocks per SM (register bound)
   __host__ __device__ static int key_comp(int i) { return 2; }
   __host__ __device__ static int vel_comp(int i) { return -1; }
 };
@@ -51,7 +51,7 @@ template <> struct Robot<DPG_ROBOT_CAR1> {
   static constexpr bool ROLLOUT = false, SPHERE = false;
   static constexpr int KEYD = 2;  // theta0, theta1
   static constexpr int CHUNK = 8;
-  static constexpr int CHECK_BLOCKS = 4;
+  static constexpr int CHECK_BLOCKS = 4;  // measured: 4 beats 3, 5 and 6 here
   __host__ __device__ static int key_comp(int i) { return 2 + i; }
   __host__ __device__ static int vel_comp(int i) { return -1; }
 };
