@@ -168,7 +168,9 @@ __device__ __forceinline__ bool near_box(const float *cen, const float *hf, cons
 
 // ------------------------------------------------------------- one pair ----
 
-template <int KIND, class Real, bool BAND, bool CULL, bool LOCKSTEP>
+// NW: words of the per-lane obstacle bitmasks (obstacles <= 32 NW); 0 = no
+// culling (more than kMaxCullObs obstacles), every state tests every obstacle.
+template <int KIND, class Real, bool BAND, int NW, bool LOCKSTEP>
 __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t pair, uint32_t node,
                           bool active) {
   using R = Robot<KIND>;
@@ -220,7 +222,9 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   }
 
   // level-1 culling: obstacles near the whole transformed primitive
-  uint32_t l1[kMaxCullObs / 32] = {0u, 0u, 0u, 0u};
+  constexpr bool CULL = NW > 0;
+  constexpr int NWA = NW > 0 ? NW : 1;
+  uint32_t l1[NWA] = {};
   const float M = A.cull_margin;
   if (CULL && active) {
     const float *tb = pv.tbox32 + (int64_t)p * 2 * D;
@@ -236,8 +240,14 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
         hf[i] += 0.5f * fabsf(sv);
       }
     }
-    for (int o = 0; o < n_obs; o++)
-      if (near_box<D, Real>(cen, hf, obs_sm, o, M)) l1[o >> 5] |= 1u << (o & 31);
+#pragma unroll
+    for (int w = 0; w < NWA; w++) {  // word by word: the masks stay in registers
+      uint32_t bits = 0u;
+      const int o0 = 32 * w, o1 = min(n_obs, o0 + 32);
+      for (int o = o0; o < o1; o++)
+        if (near_box<D, Real>(cen, hf, obs_sm, o, M)) bits |= 1u << (o - o0);
+      l1[w] = bits;
+    }
   }
 
   bool done = !active, collided = false, rechecked = false;
@@ -246,7 +256,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   const Real hl = F32 ? Real(A.half_len32) : Real(rp.half_len);
   const Real hw = F32 ? Real(A.half_wid32) : Real(rp.half_wid);
   const Real rad = F32 ? Real(A.radius32) : Real(rp.radius);
-  uint32_t cm[kMaxCullObs / 32] = {0u, 0u, 0u, 0u};
+  uint32_t cm[NWA] = {};
   bool nb = need_bounds;  // bounds tests in the current chunk
 
   for (int k = 0; k < L; k++) {
@@ -274,7 +284,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
       }
       if (!done && !collided) {
 #pragma unroll
-        for (int w = 0; w < kMaxCullObs / 32; w++) {
+        for (int w = 0; w < NWA; w++) {
           uint32_t m = l1[w], c = 0;
           while (m) {
             const int b = __ffs(m) - 1;
@@ -296,7 +306,10 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
       // no lane has an obstacle test or a bounds test to make in this chunk:
       // its states change nothing (no contact, no bound, no min_gap update)
       if (LOCKSTEP) {
-        const bool idle = done || ((collided || (cm[0] | cm[1] | cm[2] | cm[3]) == 0u) && !nb);
+        uint32_t any = 0u;
+#pragma unroll
+        for (int w = 0; w < NWA; w++) any |= cm[w];
+        const bool idle = done || ((collided || any == 0u) && !nb);
         if (__all_sync(kFull, idle)) {
           k += R::CHUNK - 1;
           continue;
@@ -356,7 +369,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
     };
     if (CULL) {
 #pragma unroll
-      for (int w = 0; w < kMaxCullObs / 32; w++) {
+      for (int w = 0; w < NWA; w++) {
         uint32_t m = cm[w];
         while (m) {
           const int b = __ffs(m) - 1;
@@ -426,7 +439,7 @@ __device__ void load_obstacles(const EnvView &ev, void *sm) {
 }
 
 // Persistent warps over (primitive, 32 nodes) work items.
-template <int KIND, class Real, bool BAND, bool CULL>
+template <int KIND, class Real, bool BAND, int NW>
 __global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) check_pairs(CheckArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   load_obstacles<Real, KIND>(A.ev, smem);
@@ -460,7 +473,7 @@ __global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) chec
     const unsigned long long pair = first + lane;
     const bool active = pair < end;
     const uint32_t node = active ? A.out.node[pair] : 0u;
-    check_one<KIND, Real, BAND, CULL, true>(A, smem, p, (int64_t)pair, node, active);
+    check_one<KIND, Real, BAND, NW, true>(A, smem, p, (int64_t)pair, node, active);
   }
 }
 

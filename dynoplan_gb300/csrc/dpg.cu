@@ -115,7 +115,9 @@ template <class F> void with_kind(int kind, F &&f) {
 template <int KIND>
 static void launch_check(dpg_ctx *c, const CheckArgs &ca, bool fp64, cudaStream_t st) {
   using R = Robot<KIND>;
-  const bool cull = c->n_obs <= kMaxCullObs;
+  // obstacle bitmask words per lane: the fewest that cover the obstacles
+  // (fewer registers), none above kMaxCullObs (no culling)
+  const int nw = c->n_obs <= 32 ? 1 : c->n_obs <= 64 ? 2 : c->n_obs <= 96 ? 3 : c->n_obs <= kMaxCullObs ? 4 : 0;
   const size_t ob = fp64 ? (R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>))
                          : (R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>));
   const size_t sm = ob * std::max(c->n_obs, 1);
@@ -125,13 +127,19 @@ static void launch_check(dpg_ctx *c, const CheckArgs &ca, bool fp64, cudaStream_
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
     kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
   };
-  if (fp64) {
-    if (cull) go(check_pairs<KIND, double, false, true>);
-    else go(check_pairs<KIND, double, false, false>);
-  } else {
-    if (cull) go(check_pairs<KIND, float, true, true>);
-    else go(check_pairs<KIND, float, true, false>);
-  }
+  auto by_words = [&](auto real, auto band) {
+    using Real = decltype(real);
+    constexpr bool BAND = decltype(band)::value;
+    switch (nw) {
+      case 1: go(check_pairs<KIND, Real, BAND, 1>); break;
+      case 2: go(check_pairs<KIND, Real, BAND, 2>); break;
+      case 3: go(check_pairs<KIND, Real, BAND, 3>); break;
+      case 4: go(check_pairs<KIND, Real, BAND, 4>); break;
+      default: go(check_pairs<KIND, Real, BAND, 0>); break;
+    }
+  };
+  if (fp64) by_words(0.0, std::false_type{});
+  else by_words(0.0f, std::true_type{});
 }
 
 // primitive tiles per nn_mask block: small node batches are split over the
