@@ -39,8 +39,9 @@ sys.path.insert(0, ROOT)
 METRIC = "checked (node,primitive) expansions/s"
 UNIT = "pairs/s"
 # node_cells cell_scan cell_scatter cell_sort gather_nodes (spatial order, batches of
-# >= 2048 nodes) prep_nodes nn_mask nn_prefix scan_totals nn_emit check_pairs unpermute_nodes
-KERNELS_PER_STEP = 12
+# >= 2048 nodes) prep_nodes nn_grid (key-grid ball scan; nn_mask for the quadrotor)
+# nn_prefix scan_totals nn_emit check_pairs (which also restores the node ids)
+KERNELS_PER_STEP = 11
 L2_FLUSH_BYTES = 512 << 20
 
 # DRAM bytes per check_pairs launch from ncu (dram__bytes_read.sum +

@@ -49,6 +49,12 @@ struct CheckArgs {
   // double->float conversions at 1/64 of the FP32 rate)
   float dt32, half_len32, half_wid32, radius32, band32;
   float lo32[3], hi32[3];
+  // this launch takes work items [n_items sub / nsub, n_items (sub + 1) / nsub)
+  // (nsub 0 = 1: all items)
+  int sub, nsub;
+  // when set, the pair's node id is written back through it (processing
+  // order -> caller's numbering) once the pair is checked
+  const uint32_t *perm;
 };
 
 template <class Real> __device__ __forceinline__ const Pose<Real> *pose_table(const PrimView &pv);
@@ -391,6 +397,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   if (LOCKSTEP && (threadIdx.x & 31) == 0 && rmask) atomicAdd(&A.ctr->n_recheck, (unsigned long long)__popc(rmask));
   if (!active) return;
   const PairView &o = A.out;
+  if (A.perm) o.node[pair] = A.perm[node];
   uint8_t verdict;
   int fi;
   if (first_oob < L) { verdict = DPG_OUT_OF_BOUNDS; fi = first_oob; }
@@ -445,13 +452,15 @@ __global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) chec
   load_obstacles<Real, KIND>(A.ev, smem);
   const int lane = threadIdx.x & 31;
   const int P = A.pv.P;
-  const unsigned long long n_items = A.ctr->n_items;
+  const unsigned long long n_all = A.ctr->n_items;
+  const int nsub = A.nsub > 0 ? A.nsub : 1;
+  const unsigned long long i_lo = n_all * A.sub / nsub, n_items = n_all * (A.sub + 1) / nsub;
   while (true) {
     unsigned long long item = 0;
     int stop = 0;
     if (lane == 0) {
       stop = *A.abort_flag;
-      item = stop ? n_items : atomicAdd(&A.ctr->next_item, 1ull);
+      item = stop ? n_items : i_lo + atomicAdd(&A.ctr->next_sub[A.sub], 1ull);
     }
     item = __shfl_sync(kFull, item, 0);
     stop = __shfl_sync(kFull, stop, 0);

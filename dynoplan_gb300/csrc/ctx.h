@@ -48,7 +48,16 @@ struct dpg_ctx {
   DevBuf q_node, q_prim, q_sorted, q_idx, q_fill;  // dpg_check_pairs
   DevBuf ord_cell, ord_perm, ord_cnt, ord_start, ord_fill, x64s;  // spatial order of a batch
   dpg::DevCounters *d_ctr = nullptr;
-  dpg::DevCounters *h_ctr = nullptr;  // pinned
+  dpg::DevCounters *h_ctr = nullptr;  // pinned, 2 entries: after the ball scan, at the end
+  // host-buffer expands: result copies overlap the check (copy stream, one
+  // event per check launch, pinned mirrors of the item / pair bases)
+  cudaStream_t cstream = nullptr;
+  cudaStream_t xstream = nullptr;  // every other check launch, so one drains while the next fills
+  cudaEvent_t ev_ball = nullptr;
+  cudaEvent_t ev_sub[dpg::kMaxSub] = {};
+  cudaEvent_t ev_tot = nullptr;
+  unsigned long long *h_bases = nullptr;  // [2][h_bases_n]: ord_ibase, ord_pbase
+  size_t h_bases_n = 0;
   int *h_abort = nullptr;             // mapped pinned
   int *d_abort = nullptr;
   cudaEvent_t ev[6] = {};

@@ -158,6 +158,8 @@ static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
 // primitive (split over the primitives too, to fill the GPU).  Both give the
 // same mask and counts.
 constexpr int64_t kGridMin = 2048;
+constexpr int kPipe = 8;  // check launches of an expand whose results go to host buffers
+static_assert(kPipe <= kMaxSub, "one work-queue counter per check launch");
 template <int KIND>
 static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv, double radius, double ball_band,
                         int Ppad, int64_t B, int64_t W, uint32_t *mask, uint32_t *cnt, uint32_t *tot,
@@ -275,7 +277,7 @@ int dpg_create(dpg_ctx **out, int device, const dpg_robot_desc *robot) {
     // default stream, which produces device-resident inputs
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamDefault) != cudaSuccess) { rc = DPG_ERR_CUDA; break; }
     if (cudaMalloc(&c->d_ctr, sizeof(DevCounters)) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
-    if (cudaHostAlloc(&c->h_ctr, sizeof(DevCounters), cudaHostAllocDefault) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
+    if (cudaHostAlloc(&c->h_ctr, 2 * sizeof(DevCounters), cudaHostAllocDefault) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
     if (cudaHostAlloc(&c->h_abort, sizeof(int), cudaHostAllocMapped) != cudaSuccess) { rc = DPG_ERR_OOM; break; }
     *c->h_abort = 0;
     if (cudaHostGetDevicePointer(&c->d_abort, c->h_abort, 0) != cudaSuccess) { rc = DPG_ERR_CUDA; break; }
@@ -294,6 +296,8 @@ void dpg_destroy(dpg_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->cstream) cudaStreamSynchronize(c->cstream);
+  if (c->xstream) cudaStreamSynchronize(c->xstream);
   DevBuf *bufs[] = {&c->len, &c->soff, &c->aoff, &c->order, &c->key32, &c->kconst32, &c->st64,
                     &c->st32, &c->act64, &c->pose32, &c->pose64, &c->pbox, &c->pbox32, &c->obs32, &c->obs64,
                     &c->x64, &c->nkey32, &c->noff32, &c->mask, &c->cnt, &c->tot, &c->pbase,
@@ -305,6 +309,13 @@ void dpg_destroy(dpg_ctx *c) {
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
+  if (c->h_bases) cudaFreeHost(c->h_bases);
+  for (auto &e : c->ev_sub)
+    if (e) cudaEventDestroy(e);
+  if (c->ev_tot) cudaEventDestroy(c->ev_tot);
+  if (c->ev_ball) cudaEventDestroy(c->ev_ball);
+  if (c->cstream) cudaStreamDestroy(c->cstream);
+  if (c->xstream) cudaStreamDestroy(c->xstream);
   if (c->h_abort) cudaFreeHost(c->h_abort);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -660,6 +671,27 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     pv_out.flags = out->flags ? P_<uint8_t>(c->p_flags) : nullptr;
   }
 
+  // host-buffer outputs of a checked batch in spatial order: the check runs as
+  // kPipe launches over item ranges and each range's results are copied out
+  // while the next range is checked
+  const bool pipelined = !dev_out && !(opts->mode & DPG_MODE_BALL_ONLY) && reorder && cap > 0;
+  if (pipelined) {
+    if (!c->cstream) {
+      CUDA_TRY(c, cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
+      CUDA_TRY(c, cudaStreamCreateWithFlags(&c->xstream, cudaStreamNonBlocking));
+      for (auto &e : c->ev_sub) CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_tot, cudaEventDisableTiming));
+      CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_ball, cudaEventDisableTiming));
+    }
+    if (c->h_bases_n < (size_t)P + 1) {
+      if (c->h_bases) cudaFreeHost(c->h_bases);
+      c->h_bases = nullptr;
+      c->h_bases_n = 0;
+      CUDA_TRY(c, cudaHostAlloc(&c->h_bases, 2 * sizeof(unsigned long long) * (P + 1), cudaHostAllocDefault));
+      c->h_bases_n = (size_t)P + 1;
+    }
+  }
+
   CUDA_TRY(c, cudaEventRecord(c->ev[0], st));
   if (N > 0) {
     if (opts->x_on_device)
@@ -756,20 +788,83 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
                                   P_<unsigned long long>(c->pbase), cap, pv_out.node, pv_out.prim);
     }
     cudaEventRecord(c->ev[2], st);
-    // exact check: persistent grid, obstacles in shared memory
-    if (!(opts->mode & DPG_MODE_BALL_ONLY)) launch_check<KIND>(c, ca, fp64, st);  // ball-only: pairs, no check
-    if (reorder && cap > 0)
+    launch_err = cudaGetLastError();
+  });
+  if (launch_err != cudaSuccess)
+    return fail(c, DPG_ERR_CUDA, std::string("expand launch: ") + cudaGetErrorString(launch_err));
+  if (pipelined) {  // what the host needs to place the copies: counters and item / pair bases
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_ctr, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_bases, c->ord_ibase.p, sizeof(unsigned long long) * (P + 1),
+                                cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_bases + c->h_bases_n, c->ord_pbase.p, sizeof(unsigned long long) * (P + 1),
+                                cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaEventRecord(c->ev_tot, st));
+    CUDA_TRY(c, cudaEventRecord(c->ev_ball, st));
+    CUDA_TRY(c, cudaStreamWaitEvent(c->xstream, c->ev_ball, 0));
+  }
+  with_kind(kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    if (!(opts->mode & DPG_MODE_BALL_ONLY)) {
+      // exact check: persistent grid, obstacles in shared memory; node ids go
+      // back to the caller's numbering as each pair is done.  Pipelined: the
+      // launches alternate between two streams (disjoint item ranges and
+      // work-queue counters), so the next range's blocks take the SMs that
+      // the previous range's last items leave idle
+      ca.perm = reorder ? P_<uint32_t>(c->ord_perm) : nullptr;
+      ca.nsub = pipelined ? kPipe : 1;
+      for (int j = 0; j < ca.nsub; j++) {
+        ca.sub = j;
+        cudaStream_t s = pipelined && (j & 1) ? c->xstream : st;
+        launch_check<KIND>(c, ca, fp64, s);
+        if (pipelined) cudaEventRecord(c->ev_sub[j], s);
+      }
+      if (pipelined) {  // join: the last launch on the second stream
+        const int last_x = ca.nsub % 2 == 0 ? ca.nsub - 1 : ca.nsub - 2;
+        cudaStreamWaitEvent(st, c->ev_sub[last_x], 0);
+      }
+    } else if (reorder && cap > 0) {  // ball only: pairs, no check
       unpermute_nodes<<<(unsigned)((cap + 255) / 256), 256, 0, st>>>(ctr, cap, P_<uint32_t>(c->ord_perm),
                                                                     pv_out.node);
+    }
     cudaEventRecord(c->ev[3], st);
     cudaEventRecord(c->ev[4], st);
     launch_err = cudaGetLastError();
   });
   if (launch_err != cudaSuccess)
     return fail(c, DPG_ERR_CUDA, std::string("expand launch: ") + cudaGetErrorString(launch_err));
-  CUDA_TRY(c, cudaMemcpyAsync(c->h_ctr, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+  if (pipelined) {
+    // copy each check launch's pairs (a contiguous range: items are laid out
+    // in pair order) on the copy stream as soon as that launch is done
+    CUDA_TRY(c, cudaEventSynchronize(c->ev_tot));
+    const DevCounters h0 = c->h_ctr[0];
+    if (!h0.n_overflow && h0.n_pairs > 0) {
+      const unsigned long long *ib = c->h_bases, *pb = c->h_bases + c->h_bases_n;
+      auto pair_at = [&](unsigned long long item) -> int64_t {
+        if (item >= h0.n_items) return (int64_t)h0.n_pairs;
+        const int lo = (int)(std::upper_bound(ib, ib + P, item) - ib) - 1;  // ib[lo] <= item < ib[lo + 1]
+        return (int64_t)(pb[lo] + 32ull * (item - ib[lo]));
+      };
+      struct { void *dst; void *src; size_t b; } cp[] = {
+          {out->node, c->p_node.p, 4}, {out->prim, c->p_prim.p, 4}, {out->verdict, c->p_verdict.p, 1},
+          {out->first_invalid, c->p_fi.p, 2}, {out->end_state, c->p_end.p, es_bytes * nx},
+          {out->min_gap, c->p_gap.p, 4}, {out->flags, c->p_flags.p, 1}};
+      for (int j = 0; j < kPipe; j++) {
+        const int64_t a = pair_at(h0.n_items * j / kPipe), e = pair_at(h0.n_items * (j + 1) / kPipe);
+        CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev_sub[j], 0));
+        if (e > a)
+          for (const auto &f : cp)
+            if (f.dst)
+              CUDA_TRY(c, cudaMemcpyAsync(static_cast<char *>(f.dst) + a * f.b, static_cast<char *>(f.src) + a * f.b,
+                                          (e - a) * f.b, cudaMemcpyDeviceToHost, c->cstream));
+      }
+    }
+    CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev[4], 0));
+    CUDA_TRY(c, cudaEventRecord(c->ev[5], c->cstream));
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_ctr + 1, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(c, cudaStreamSynchronize(st));
-  const DevCounters h = *c->h_ctr;
+  if (pipelined) CUDA_TRY(c, cudaStreamSynchronize(c->cstream));
+  const DevCounters h = c->h_ctr[1];
   out->n_pairs = (int64_t)h.n_pairs;
   out->n_scanned = N * (int64_t)P;
   out->n_contact_recheck = (int64_t)h.n_recheck;
@@ -777,7 +872,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   if (h.status == DPG_ERR_ABORTED) return fail(c, DPG_ERR_ABORTED, "expand: aborted");
   if ((int64_t)h.n_pairs > cap) return fail(c, DPG_ERR_CAPACITY, "expand: output capacity too small");
   const int64_t np = (int64_t)h.n_pairs;
-  if (!dev_out && np > 0) {
+  if (pipelined) {
+    // copied above
+  } else if (!dev_out && np > 0) {
     struct { void *dst; void *src; size_t b; } cp[] = {
         {out->node, c->p_node.p, 4}, {out->prim, c->p_prim.p, 4}, {out->verdict, c->p_verdict.p, 1},
         {out->first_invalid, c->p_fi.p, 2}, {out->end_state, c->p_end.p, es_bytes * nx},
@@ -785,11 +882,11 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     const int n_copy = (opts->mode & DPG_MODE_BALL_ONLY) ? 2 : 7;  // pairs only: node, prim
     for (int i = 0; i < n_copy; i++)
       if (cp[i].dst) CUDA_TRY(c, cudaMemcpyAsync(cp[i].dst, cp[i].src, cp[i].b * np, cudaMemcpyDeviceToHost, st));
-  } else if (dev_out && np > 0) {
-    // node / prim live in the arena unless the caller gave arrays
   }
-  CUDA_TRY(c, cudaEventRecord(c->ev[5], st));
-  CUDA_TRY(c, cudaStreamSynchronize(st));
+  if (!pipelined) {
+    CUDA_TRY(c, cudaEventRecord(c->ev[5], st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+  }
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->timings[0] = ms;
   cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); c->timings[1] = ms;

@@ -35,10 +35,12 @@ constexpr int kCheckThreads = 256;
 constexpr int kMaxCullObs = 128;   // per-lane candidate bitmask covers this many obstacles
 constexpr float kGapCap = 0.05f;   // min_gap is exact up to this clearance, +inf above
 
+constexpr int kMaxSub = 8;  // check launches per expand (item ranges)
+
 struct DevCounters {
   unsigned long long n_pairs;
   unsigned long long n_items;
-  unsigned long long next_item;
+  unsigned long long next_sub[kMaxSub];  // work-queue position of each check launch
   unsigned long long n_recheck;
   unsigned long long n_ball_recheck;
   unsigned long long n_overflow;
@@ -500,7 +502,7 @@ static __global__ void __launch_bounds__(1024) scan_totals(int P, const int32_t 
     const bool overflow = (int64_t)sp[T - 1] > cap;
     ctr->n_overflow = overflow ? 1 : 0;
     ctr->n_items = overflow ? 0 : si[T - 1];
-    ctr->next_item = 0;
+    for (int i = 0; i < kMaxSub; i++) ctr->next_sub[i] = 0;
   }
 }
 
