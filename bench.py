@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "checked (node,primitive) expansions/s"
 UNIT = "pairs/s"
-# node_cells cell_scan cell_scatter cell_sort gather_nodes (spatial order, batches of
+# node_tiles nn_prefix cell_scan cell_scatter gather_nodes (spatial order, batches of
 # >= 2048 nodes) prep_nodes nn_grid (key-grid ball scan; nn_mask for the quadrotor)
 # nn_prefix scan_totals nn_emit check_pairs (which also restores the node ids)
 KERNELS_PER_STEP = 11

@@ -46,7 +46,7 @@ struct dpg_ctx {
   DevBuf x64, nkey32, noff32, mask, cnt, tot, pbase, ord_pbase, ord_ibase;
   DevBuf p_node, p_prim, p_verdict, p_fi, p_end, p_gap, p_flags;
   DevBuf q_node, q_prim, q_sorted, q_idx, q_fill;  // dpg_check_pairs
-  DevBuf ord_cell, ord_perm, ord_cnt, ord_start, ord_fill, x64s;  // spatial order of a batch
+  DevBuf ord_cell, ord_perm, ord_cnt, ord_start, ord_rank, ord_tiles, x64s;  // spatial order of a batch
   dpg::DevCounters *d_ctr = nullptr;
   dpg::DevCounters *h_ctr = nullptr;  // pinned, 2 entries: after the ball scan, at the end
   // host-buffer expands: result copies overlap the check (copy stream, one

@@ -152,7 +152,8 @@ static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
 }
 
 // Ball scan of the nv.N nodes against the pv.P primitives: bitmask words
-// (W x Ppad), per-tile counts cnt[B][P] turned into prefixes, totals tot[P].
+// (P x Wpad, primitive-major), per-tile counts cnt[B][P] turned into prefixes,
+// totals tot[P].
 // Batches of at least kGridMin nodes of a robot with a key grid test only the
 // primitives of the cells near their key; smaller batches test every
 // primitive (split over the primitives too, to fill the GPU).  Both give the
@@ -162,7 +163,7 @@ constexpr int kPipe = 8;  // check launches of an expand whose results go to hos
 static_assert(kPipe <= kMaxSub, "one work-queue counter per check launch");
 template <int KIND>
 static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv, double radius, double ball_band,
-                        int Ppad, int64_t B, int64_t W, uint32_t *mask, uint32_t *cnt, uint32_t *tot,
+                        int64_t Wpad, int64_t B, int64_t W, uint32_t *mask, uint32_t *cnt, uint32_t *tot,
                         DevCounters *ctr, cudaStream_t st) {
   using R = Robot<KIND>;
   const RobotParams &rp = c->rp;
@@ -180,14 +181,14 @@ static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv
       };
       const float h0 = half(rp.w[1], true);
       const float h1 = half(KIND == DPG_ROBOT_CAR1 ? rp.w[2] : rp.w[3], KIND == DPG_ROBOT_CAR1);
-      cudaMemsetAsync(mask, 0, sizeof(uint32_t) * (size_t)W * Ppad, st);
+      cudaMemsetAsync(mask, 0, sizeof(uint32_t) * (size_t)P * Wpad, st);
       if (P <= kGridSmemP) {
         nn_grid<KIND, true><<<(unsigned)B, kNNThreads, sizeof(uint32_t) * P, st>>>(
-            rp, pv, nv, c->kg, w32, (float)radius, radius, (float)ball_band, h0, h1, Ppad, mask, cnt, ctr);
+            rp, pv, nv, c->kg, w32, (float)radius, radius, (float)ball_band, h0, h1, Wpad, mask, cnt, ctr);
       } else {
         cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (size_t)B * P, st);
         nn_grid<KIND, false><<<(unsigned)B, kNNThreads, 0, st>>>(rp, pv, nv, c->kg, w32, (float)radius, radius,
-                                                                 (float)ball_band, h0, h1, Ppad, mask, cnt, ctr);
+                                                                 (float)ball_band, h0, h1, Wpad, mask, cnt, ctr);
       }
       done = true;
     }
@@ -195,7 +196,7 @@ static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv
   if (!done) {
     const int tpy = nn_tiles_per_y(P, B, c->sm_count);
     const dim3 ng((unsigned)B, (unsigned)((P + tpy * kNNTile - 1) / (tpy * kNNTile)));
-    nn_mask<KIND><<<ng, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)radius, radius, (float)ball_band, Ppad, tpy,
+    nn_mask<KIND><<<ng, kNNThreads, 0, st>>>(rp, pv, nv, w32, (float)radius, radius, (float)ball_band, Wpad, tpy,
                                              mask, cnt, ctr);
   }
   nn_prefix<<<(unsigned)((P + 31) / 32), 256, 0, st>>>(P, (int)B, cnt, tot);
@@ -304,7 +305,7 @@ void dpg_destroy(dpg_ctx *c) {
                     &c->ord_pbase, &c->ord_ibase, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
                     &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32,
                     &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill,
-                    &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_fill, &c->x64s,
+                    &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_rank, &c->ord_tiles, &c->x64s,
                     &c->kg_start, &c->kg_tab};
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
@@ -617,8 +618,8 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   const int kd = key_dim(kind), od = off_dim(kind);
   const bool fp64 = opts->precision == DPG_FP64;
   const int64_t cap = out->capacity;
-  const int Ppad = (P + 31) / 32 * 32;
   const int64_t W = (N + 31) / 32;
+  const int64_t Wpad = (W + 31) / 32 * 32;  // mask row: words of a primitive, whole emit groups
   const int64_t B = (N + kNNThreads - 1) / kNNThreads;
   const size_t es_bytes = fp64 ? sizeof(double) : sizeof(float);
   cudaStream_t st = c->stream;
@@ -626,7 +627,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   if ((rc = ensure(c, c->x64, sizeof(double) * nx * std::max<int64_t>(N, 1))) ||
       (rc = ensure(c, c->nkey32, sizeof(float) * kd * std::max<int64_t>(N, 1))) ||
       (rc = ensure(c, c->noff32, sizeof(float) * od * std::max<int64_t>(N, 1))) ||
-      (rc = ensure(c, c->mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(W, 1) * Ppad)) ||
+      (rc = ensure(c, c->mask, sizeof(uint32_t) * (size_t)std::max<int64_t>(Wpad, 32) * P)) ||
       (rc = ensure(c, c->cnt, sizeof(uint32_t) * (size_t)std::max<int64_t>(B, 1) * P)) ||
       (rc = ensure(c, c->tot, sizeof(uint32_t) * P)) ||
       (rc = ensure(c, c->pbase, sizeof(unsigned long long) * P)) ||
@@ -639,7 +640,8 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       ((rc = ensure(c, c->ord_cell, sizeof(uint32_t) * N)) || (rc = ensure(c, c->ord_perm, sizeof(uint32_t) * N)) ||
        (rc = ensure(c, c->ord_cnt, sizeof(uint32_t) * kOrderCells)) ||
        (rc = ensure(c, c->ord_start, sizeof(uint32_t) * kOrderCells)) ||
-       (rc = ensure(c, c->ord_fill, sizeof(uint32_t) * kOrderCells)) ||
+       (rc = ensure(c, c->ord_rank, sizeof(uint32_t) * N)) ||
+       (rc = ensure(c, c->ord_tiles, sizeof(uint32_t) * kOrderCells * (size_t)((N + order_tile(N) - 1) / order_tile(N)))) ||
        (rc = ensure(c, c->x64s, sizeof(double) * nx * N))))
     return rc;
   // pair arrays: the caller's device arrays when given, else the arena
@@ -758,15 +760,15 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     using R = Robot<KIND>;
     if (reorder) {  // nodes by Z-order cell, then index; the pipeline runs on the sorted copy
       const unsigned nb = (unsigned)((N + 255) / 256);
-      cudaMemsetAsync(c->ord_cnt.p, 0, sizeof(uint32_t) * kOrderCells, st);
-      cudaMemsetAsync(c->ord_fill.p, 0, sizeof(uint32_t) * kOrderCells, st);
-      node_cells<KIND><<<nb, 256, 0, st>>>(P_<double>(c->x64), N, ev, P_<uint32_t>(c->ord_cell),
-                                           P_<uint32_t>(c->ord_cnt));
+      const int64_t tile = order_tile(N), ntile = (N + tile - 1) / tile;
+      node_tiles<KIND><<<(unsigned)ntile, 256, 0, st>>>(P_<double>(c->x64), N, ev, tile, P_<uint32_t>(c->ord_cell),
+                                                         P_<uint32_t>(c->ord_rank), P_<uint32_t>(c->ord_tiles));
+      nn_prefix<<<kOrderCells / 32, 256, 0, st>>>(kOrderCells, (int)ntile, P_<uint32_t>(c->ord_tiles),
+                                                  P_<uint32_t>(c->ord_cnt));
       cell_scan<<<1, 1024, 0, st>>>(kOrderCells, P_<uint32_t>(c->ord_cnt), P_<uint32_t>(c->ord_start));
-      cell_scatter<<<nb, 256, 0, st>>>(N, P_<uint32_t>(c->ord_cell), P_<uint32_t>(c->ord_start),
-                                       P_<uint32_t>(c->ord_fill), P_<uint32_t>(c->ord_perm));
-      cell_sort<<<kOrderCells * 32 / 256, 256, 0, st>>>(kOrderCells, P_<uint32_t>(c->ord_start),
-                                                        P_<uint32_t>(c->ord_cnt), P_<uint32_t>(c->ord_perm));
+      cell_scatter<<<nb, 256, 0, st>>>(N, tile, P_<uint32_t>(c->ord_cell), P_<uint32_t>(c->ord_rank),
+                                       P_<uint32_t>(c->ord_tiles), P_<uint32_t>(c->ord_start),
+                                       P_<uint32_t>(c->ord_perm));
       gather_nodes<R::NX><<<(unsigned)((N * R::NX + 255) / 256), 256, 0, st>>>(
           P_<double>(c->x64), P_<uint32_t>(c->ord_perm), N, P_<double>(c->x64s));
       nv.x64 = P_<double>(c->x64s);
@@ -774,7 +776,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     }
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
-      launch_ball<KIND>(c, pv, nv, opts->radius, ball_band, Ppad, B, W, P_<uint32_t>(c->mask),
+      launch_ball<KIND>(c, pv, nv, opts->radius, ball_band, Wpad, B, W, P_<uint32_t>(c->mask),
                         P_<uint32_t>(c->cnt), P_<uint32_t>(c->tot), ctr, st);
     } else {
       cudaMemsetAsync(c->tot.p, 0, sizeof(uint32_t) * P, st);
@@ -783,9 +785,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
                                     P_<unsigned long long>(c->pbase), P_<unsigned long long>(c->ord_pbase),
                                     P_<unsigned long long>(c->ord_ibase), cap, ctr);
     if (N > 0) {
-      dim3 eg((unsigned)((Ppad / 32 + 7) / 8), (unsigned)B);
-      nn_emit<<<eg, 256, 0, st>>>(P, Ppad, W, P_<uint32_t>(c->mask), P_<uint32_t>(c->cnt),
-                                  P_<unsigned long long>(c->pbase), cap, pv_out.node, pv_out.prim);
+      nn_emit<<<(unsigned)((P * (Wpad / 32) + 7) / 8), 256, 0, st>>>(
+          P, W, Wpad, P_<uint32_t>(c->mask), P_<uint32_t>(c->cnt), P_<unsigned long long>(c->pbase), cap,
+          pv_out.node, pv_out.prim);
     }
     cudaEventRecord(c->ev[2], st);
     launch_err = cudaGetLastError();
@@ -966,15 +968,15 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
   const int kd = key_dim(kind), od = off_dim(kind);
   const bool fp64 = opts->precision == DPG_FP64;
   const int64_t cap = out->capacity;
-  const int Ppad = (P + 31) / 32 * 32;
   const int64_t W = (N + 31) / 32;
+  const int64_t Wpad = (W + 31) / 32 * 32;
   const int64_t B = (N + kNNThreads - 1) / kNNThreads;
 
   // carve the scratch; reject sizes beyond the array
   size_t off_key = 0;
   size_t off_off = off_key + align256(sizeof(float) * kd * (size_t)N);
   size_t off_mask = off_off + align256(sizeof(float) * od * (size_t)N);
-  size_t off_cnt = off_mask + align256(sizeof(uint32_t) * (size_t)W * Ppad);
+  size_t off_cnt = off_mask + align256(sizeof(uint32_t) * (size_t)Wpad * P);
   size_t off_tot = off_cnt + align256(sizeof(uint32_t) * (size_t)B * P);
   size_t off_pbase = off_tot + align256(sizeof(uint32_t) * (size_t)P);
   size_t off_opb = off_pbase + align256(sizeof(unsigned long long) * (size_t)P);
@@ -1061,14 +1063,14 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
     using R = Robot<KIND>;
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
-      launch_ball<KIND>(c, pv, nv, opts->radius, ball_band, Ppad, B, W, mask, cnt, tot, ctr, st);
+      launch_ball<KIND>(c, pv, nv, opts->radius, ball_band, Wpad, B, W, mask, cnt, tot, ctr, st);
     } else {
       cudaMemsetAsync(tot, 0, sizeof(uint32_t) * P, st);
     }
     scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), tot, pbase, ord_pbase, ord_ibase, cap, ctr);
     if (N > 0) {
-      dim3 eg((unsigned)((Ppad / 32 + 7) / 8), (unsigned)B);
-      nn_emit<<<eg, 256, 0, st>>>(P, Ppad, W, mask, cnt, pbase, cap, po.node, po.prim);
+      nn_emit<<<(unsigned)((P * (Wpad / 32) + 7) / 8), 256, 0, st>>>(P, W, Wpad, mask, cnt, pbase, cap, po.node,
+                                                                    po.prim);
     }
     launch_check<KIND>(c, ca, fp64, st);
     launch_err = cudaGetLastError();

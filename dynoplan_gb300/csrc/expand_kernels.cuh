@@ -6,7 +6,7 @@
 //                   prim) counts; FP64 re-test of |d - r| <= ball_band
 //   nn_prefix       per-primitive exclusive prefix over node tiles
 //   scan_totals     per-primitive bases in length order, work-item bases
-//   (node_cells, cell_scan, cell_scatter, cell_sort, gather_nodes: batches
+//   (node_tiles, nn_prefix, cell_scan, cell_scatter, gather_nodes: batches
 //    of >= kReorderMin nodes are processed in spatial order)
 //   nn_emit         pair lists grouped by primitive, nodes in processing order
 //   check_pairs     persistent warps over (primitive, 32 nodes) work items
@@ -21,6 +21,7 @@
 // offset differs per lane.
 #pragma once
 
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 
@@ -140,11 +141,10 @@ __global__ void prep_nodes(NodeView nv) {
 constexpr int kOrderCells = 4096;
 constexpr int64_t kReorderMin = 2048;  // smaller batches keep the caller's order
 
+// Z-order cell of node n
 template <int KIND>
-__global__ void node_cells(const double *x64, int64_t N, EnvView ev, uint32_t *cell, uint32_t *cnt) {
+__device__ __forceinline__ uint32_t cell_code(const double *x64, int64_t n, const EnvView &ev) {
   using R = Robot<KIND>;
-  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (n >= N) return;
   constexpr int bits = R::POSD == 3 ? 4 : 6;
   uint32_t code = 0;
 #pragma unroll
@@ -156,8 +156,43 @@ __global__ void node_cells(const double *x64, int64_t N, EnvView ev, uint32_t *c
 #pragma unroll
     for (int b = 0; b < bits; b++) code |= ((q >> b) & 1u) << (R::POSD * b + d);
   }
-  cell[n] = code;
-  atomicAdd(&cnt[code], 1u);
+  return code;
+}
+
+// Stable counting sort of the nodes by cell, over tiles of `tile` consecutive
+// nodes (a multiple of 256, one block each).  node_tiles gives every node its
+// rank among the earlier nodes of its tile in the same cell, and writes the
+// tile's count per cell (cnt[b][c], every cell); nn_prefix turns the counts
+// into per-cell prefixes over the tiles and cell totals, cell_scan the totals
+// into cell starts, and cell_scatter puts node n at start[c] + prefix[b][c] +
+// rank.  The nodes of a cell come in ascending index whatever the thread
+// schedule, in O(N) for any distribution of the nodes over the cells.
+template <int KIND>
+__global__ void __launch_bounds__(256) node_tiles(const double *x64, int64_t N, EnvView ev, int64_t tile,
+                                                  uint32_t *cell, uint32_t *rank, uint32_t *cnt) {
+  __shared__ uint32_t hist[kOrderCells];
+  __shared__ uint32_t sc[256];
+  for (int c = threadIdx.x; c < kOrderCells; c += 256) hist[c] = 0u;
+  __syncthreads();
+  const int64_t t0 = blockIdx.x * tile, t1 = min(N, t0 + tile);
+  for (int64_t base = t0; base < t1; base += 256) {  // block-uniform loop over the tile's chunks
+    const int64_t n = base + threadIdx.x;
+    const bool live = n < t1;
+    const uint32_t c = live ? cell_code<KIND>(x64, n, ev) : 0xffffffffu;
+    sc[threadIdx.x] = c;
+    __syncthreads();
+    if (live) {
+      uint32_t r = hist[c];
+      for (int j = 0; j < (int)threadIdx.x; j++) r += sc[j] == c ? 1u : 0u;
+      cell[n] = c;
+      rank[n] = r;
+    }
+    __syncthreads();
+    if (live) atomicAdd(&hist[c], 1u);
+    __syncthreads();
+  }
+  uint32_t *out = cnt + (int64_t)blockIdx.x * kOrderCells;
+  for (int c = threadIdx.x; c < kOrderCells; c += 256) out[c] = hist[c];
 }
 
 // single block: start = exclusive prefix of cnt over n cells
@@ -182,50 +217,17 @@ static __global__ void __launch_bounds__(1024) cell_scan(int n, const uint32_t *
   }
 }
 
-static __global__ void cell_scatter(int64_t N, const uint32_t *cell, const uint32_t *start, uint32_t *fill,
-                                    uint32_t *perm) {
+static __global__ void cell_scatter(int64_t N, int64_t tile, const uint32_t *cell, const uint32_t *rank,
+                                    const uint32_t *tile_pre, const uint32_t *start, uint32_t *perm) {
   const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (n >= N) return;
   const uint32_t c = cell[n];
-  perm[start[c] + atomicAdd(&fill[c], 1u)] = (uint32_t)n;
+  perm[start[c] + tile_pre[(n / tile) * kOrderCells + c] + rank[n]] = (uint32_t)n;
 }
 
-// warp per cell: its nodes by ascending index, which makes the order
-// independent of the scatter's atomics.  Up to 128 nodes: rank sort in
-// registers (node indices are distinct); larger cells: one lane, insertion.
-static __global__ void cell_sort(int n_cells, const uint32_t *start, const uint32_t *cnt, uint32_t *perm) {
-  const int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-  if (c >= n_cells) return;
-  uint32_t *p = perm + start[c];
-  const uint32_t m = cnt[c];
-  if (m <= 1) return;
-  if (m <= 128) {
-    uint32_t v[4], rank[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-    for (int r = 0; r < 4; r++) v[r] = (uint32_t)(lane + 32 * r) < m ? p[lane + 32 * r] : 0xffffffffu;
-#pragma unroll
-    for (int rr = 0; rr < 4; rr++) {
-      if ((uint32_t)(32 * rr) >= m) break;
-      for (int l = 0; l < 32; l++) {
-        const uint32_t w = __shfl_sync(kFull, v[rr], l);
-#pragma unroll
-        for (int r = 0; r < 4; r++) rank[r] += (w < v[r]) ? 1u : 0u;
-      }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int r = 0; r < 4; r++)
-      if ((uint32_t)(lane + 32 * r) < m) p[rank[r]] = v[r];
-    return;
-  }
-  if (lane == 0)
-    for (uint32_t i = 1; i < m; i++) {
-      const uint32_t v = p[i];
-      uint32_t j = i;
-      for (; j > 0 && p[j - 1] > v; j--) p[j] = p[j - 1];
-      p[j] = v;
-    }
-}
+// tile length of the node sort: 256 nodes, longer for huge batches so that
+// the per-tile counts (tiles x kOrderCells) stay within 2048 tiles
+inline int64_t order_tile(int64_t N) { return 256 * std::max<int64_t>(1, (N + 256 * 2048 - 1) / (256 * 2048)); }
 
 template <int NX>
 __global__ void gather_nodes(const double *in, const uint32_t *perm, int64_t N, double *out) {
@@ -267,12 +269,13 @@ __device__ __forceinline__ float key_dist32(const float4 w, const float *nk,
 // Ball membership of 256 nodes (blockIdx.x) against the primitives of
 // `tiles_per_y` tiles of kNNTile (blockIdx.y), so that small node batches
 // still fill the GPU.
-// mask[w * Ppad + p] bit l  <=>  node 32 w + l is within radius of prim p.
+// mask[p * Wpad + w] bit l  <=>  node 32 w + l is within radius of prim p
+// (primitive-major rows of Wpad >= W words; words past W are never written).
 // cnt[b * P + p] = members of prim p among the block's nodes.
 template <int KIND>
 __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView pv, NodeView nv,
-                                                      float4 w32, float radius, double radius64, float band, int Ppad,
-                                                      int tiles_per_y, uint32_t *mask, uint32_t *cnt,
+                                                      float4 w32, float radius, double radius64, float band,
+                                                      int64_t Wpad, int tiles_per_y, uint32_t *mask, uint32_t *cnt,
                                                       DevCounters *ctr) {
   using R = Robot<KIND>;
   __shared__ float sk[R::KEYD * kNNTile];
@@ -318,7 +321,7 @@ __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView p
         if (lane == jj) mine = word;
       }
       const int p = p0 + j0 + lane;
-      if (p < Ppad && w * 32 < nv.N) mask[w * (int64_t)Ppad + p] = mine;
+      if (p < pv.P && w * 32 < nv.N) mask[(int64_t)p * Wpad + w] = mine;
       scnt[warp][j0 + lane] = __popc(mine);
     }
     __syncthreads();
@@ -358,7 +361,7 @@ constexpr int kGridSmemP = 12288;
 template <int KIND, bool SCNT>
 __global__ void __launch_bounds__(kNNThreads) nn_grid(RobotParams rp, PrimView pv, NodeView nv, KeyGrid kg,
                                                       float4 w32, float radius, double radius64, float band,
-                                                      float h0, float h1, int Ppad, uint32_t *mask, uint32_t *cnt,
+                                                      float h0, float h1, int64_t Wpad, uint32_t *mask, uint32_t *cnt,
                                                       DevCounters *ctr) {
   using R = Robot<KIND>;
   static_assert(R::KEYD <= 2, "key grid: one or two key components");
@@ -395,7 +398,6 @@ __global__ void __launch_bounds__(kNNThreads) nn_grid(RobotParams rp, PrimView p
       }
     }
     const double *xn = nv.x64 + n * R::NX;
-    uint32_t *mrow = mask + w * (int64_t)Ppad;
     const uint32_t bit = 1u << lane;
     for (int a = a0; a <= a1; a++) {
       const int ca = ((a % kg.n0) + kg.n0) % kg.n0;
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(kNNThreads) nn_grid(RobotParams rp, PrimView p
             rechecks++;
           }
           if (in) {
-            atomicOr(&mrow[p], bit);
+            atomicOr(&mask[(int64_t)p * Wpad + w], bit);
             if (SCNT) atomicAdd(&scnt[p], 1u);
             else atomicAdd(&cnt[(int64_t)blockIdx.x * pv.P + p], 1u);
           }
@@ -506,34 +508,45 @@ static __global__ void __launch_bounds__(1024) scan_totals(int P, const int32_t 
   }
 }
 
-// Warp per (node tile b, 32 primitives); lane = primitive.
-static __global__ void __launch_bounds__(256) nn_emit(int P, int Ppad, int64_t W, const uint32_t *mask,
+// Pair lists from the primitive-major bitmask.  Warp per (primitive p, group
+// g of 32 mask words = 4 node tiles); lane = word.  The warp scans the words'
+// popcounts, expands the bits into node ids in shared memory in order, and
+// writes the group's pairs as one contiguous run at pbase[p] + loc[4 g][p]
+// (the tile prefix), so the stores are coalesced.
+static __global__ void __launch_bounds__(256) nn_emit(int P, int64_t W, int64_t Wpad, const uint32_t *mask,
                                                const uint32_t *loc, const unsigned long long *pbase,
                                                int64_t cap, uint32_t *pair_node, uint32_t *pair_prim) {
-  const int lane = threadIdx.x & 31;
-  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int p = g * 32 + lane;
-  const int64_t b = blockIdx.y;
-  if (p >= P) return;
-  unsigned long long pos = pbase[p] + loc[b * P + p];
-  uint32_t words[kNNThreads / 32];  // all loads in flight before the walk
+  __shared__ uint32_t stage[8][32 * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t G = Wpad / 32;  // groups per row
+  const int64_t gw = (int64_t)blockIdx.x * 8 + warp;
+  const int64_t p = gw / G, g = gw - p * G;
+  if (p >= P) return;  // warp-uniform
+  const int64_t w = g * 32 + lane;
+  const uint32_t word = w < W ? mask[p * Wpad + w] : 0u;
+  const int c = __popc(word);
+  int incl = c;
 #pragma unroll
-  for (int k = 0; k < kNNThreads / 32; k++) {
-    const int64_t w = b * (kNNThreads / 32) + k;
-    words[k] = w < W ? mask[w * Ppad + p] : 0u;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += t;
   }
-#pragma unroll
-  for (int k = 0; k < kNNThreads / 32; k++) {
-    const int64_t w = b * (kNNThreads / 32) + k;
-    uint32_t word = words[k];
-    while (word) {
-      const int bit = __ffs(word) - 1;
-      word &= word - 1;
-      if ((int64_t)pos < cap) {
-        pair_node[pos] = (uint32_t)(w * 32 + bit);
-        pair_prim[pos] = (uint32_t)p;
-      }
-      pos++;
+  const int total = __shfl_sync(kFull, incl, 31);
+  if (total == 0) return;  // warp-uniform
+  uint32_t m = word;
+  int k = incl - c;
+  while (m) {
+    const int bit = __ffs(m) - 1;
+    m &= m - 1;
+    stage[warp][k++] = (uint32_t)(w * 32 + bit);
+  }
+  __syncwarp();
+  const unsigned long long base = pbase[p] + loc[(g * 4) * P + p];
+  for (int i = lane; i < total; i += 32) {
+    const unsigned long long pos = base + i;
+    if ((int64_t)pos < cap) {
+      pair_node[pos] = stage[warp][i];
+      pair_prim[pos] = (uint32_t)p;
     }
   }
 }
