@@ -785,7 +785,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
                                     P_<unsigned long long>(c->pbase), P_<unsigned long long>(c->ord_pbase),
                                     P_<unsigned long long>(c->ord_ibase), cap, ctr);
     if (N > 0) {
-      nn_emit<<<(unsigned)((P * (Wpad / 32) + 7) / 8), 256, 0, st>>>(
+      nn_emit<<<(unsigned)((P * ((Wpad / 32 + kEmitGroups - 1) / kEmitGroups) + 7) / 8), 256, 0, st>>>(
           P, W, Wpad, P_<uint32_t>(c->mask), P_<uint32_t>(c->cnt), P_<unsigned long long>(c->pbase), cap,
           pv_out.node, pv_out.prim);
     }
@@ -1069,8 +1069,8 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
     }
     scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), tot, pbase, ord_pbase, ord_ibase, cap, ctr);
     if (N > 0) {
-      nn_emit<<<(unsigned)((P * (Wpad / 32) + 7) / 8), 256, 0, st>>>(P, W, Wpad, mask, cnt, pbase, cap, po.node,
-                                                                    po.prim);
+      nn_emit<<<(unsigned)((P * ((Wpad / 32 + kEmitGroups - 1) / kEmitGroups) + 7) / 8), 256, 0, st>>>(
+          P, W, Wpad, mask, cnt, pbase, cap, po.node, po.prim);
     }
     launch_check<KIND>(c, ca, fp64, st);
     launch_err = cudaGetLastError();

@@ -405,20 +405,26 @@ __global__ void __launch_bounds__(kNNThreads) nn_grid(RobotParams rp, PrimView p
         const int cb = kPer1 ? ((b % kg.n1) + kg.n1) % kg.n1 : b;
         const int last = kPer1 ? min(b1, b + (kg.n1 - 1 - cb)) : b1;
         const uint32_t s = kg.start[ca * kg.n1 + cb], e = kg.start[ca * kg.n1 + cb + (last - b) + 1];
-        for (uint32_t i = s; i < e; i++) {
-          const float4 t = kg.tab[i];
-          const float sk[2] = {t.x, t.y};
-          const float d = key_dist32<KIND>(w32, nk, sk, 1, t.z);
-          bool in = d <= radius;
-          const int p = __float_as_int(t.w);
-          if (fabsf(d - radius) <= band) {  // decide in FP64
-            in = key_dist64<KIND>(rp, xn, pv.st64 + pv.soff[p] * R::NX) <= radius64;
-            rechecks++;
-          }
-          if (in) {
-            atomicOr(&mask[(int64_t)p * Wpad + w], bit);
-            if (SCNT) atomicAdd(&scnt[p], 1u);
-            else atomicAdd(&cnt[(int64_t)blockIdx.x * pv.P + p], 1u);
+        for (uint32_t i = s; i < e; i += 4) {  // four table loads in flight
+          float4 t[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) t[u] = i + u < e ? kg.tab[i + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            if (i + u >= e) break;
+            const float sk[2] = {t[u].x, t[u].y};
+            const float d = key_dist32<KIND>(w32, nk, sk, 1, t[u].z);
+            bool in = d <= radius;
+            const int p = __float_as_int(t[u].w);
+            if (fabsf(d - radius) <= band) {  // decide in FP64
+              in = key_dist64<KIND>(rp, xn, pv.st64 + pv.soff[p] * R::NX) <= radius64;
+              rechecks++;
+            }
+            if (in) {
+              atomicOr(&mask[(int64_t)p * Wpad + w], bit);
+              if (SCNT) atomicAdd(&scnt[p], 1u);
+              else atomicAdd(&cnt[(int64_t)blockIdx.x * pv.P + p], 1u);
+            }
           }
         }
         b = last + 1;
@@ -508,46 +514,64 @@ static __global__ void __launch_bounds__(1024) scan_totals(int P, const int32_t 
   }
 }
 
-// Pair lists from the primitive-major bitmask.  Warp per (primitive p, group
-// g of 32 mask words = 4 node tiles); lane = word.  The warp scans the words'
-// popcounts, expands the bits into node ids in shared memory in order, and
-// writes the group's pairs as one contiguous run at pbase[p] + loc[4 g][p]
-// (the tile prefix), so the stores are coalesced.
+// Pair lists from the primitive-major bitmask.  Warp per (primitive p, run of
+// kEmitGroups groups of 32 mask words; a group = 4 node tiles); lane = word.
+// The run's words are loaded up front (kEmitGroups loads in flight); for each
+// group the warp scans the popcounts, expands the bits into node ids in
+// shared memory in order, and writes the group's pairs as one contiguous run
+// (coalesced stores) starting at pbase[p] + loc[first tile of the run][p].
+constexpr int kEmitGroups = 8;
 static __global__ void __launch_bounds__(256) nn_emit(int P, int64_t W, int64_t Wpad, const uint32_t *mask,
                                                const uint32_t *loc, const unsigned long long *pbase,
                                                int64_t cap, uint32_t *pair_node, uint32_t *pair_prim) {
   __shared__ uint32_t stage[8][32 * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t G = Wpad / 32;  // groups per row
+  const int64_t G = Wpad / 32;                               // groups per row
+  const int64_t R = (G + kEmitGroups - 1) / kEmitGroups;     // runs per row
   const int64_t gw = (int64_t)blockIdx.x * 8 + warp;
-  const int64_t p = gw / G, g = gw - p * G;
+  const int64_t p = gw / R, g0 = (gw - p * R) * kEmitGroups;
   if (p >= P) return;  // warp-uniform
-  const int64_t w = g * 32 + lane;
-  const uint32_t word = w < W ? mask[p * Wpad + w] : 0u;
-  const int c = __popc(word);
-  int incl = c;
+  uint32_t words[kEmitGroups];
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(kFull, incl, o);
-    if (lane >= o) incl += t;
+  for (int k = 0; k < kEmitGroups; k++) {
+    const int64_t w = (g0 + k) * 32 + lane;
+    words[k] = w < W ? mask[p * Wpad + w] : 0u;
   }
-  const int total = __shfl_sync(kFull, incl, 31);
-  if (total == 0) return;  // warp-uniform
-  uint32_t m = word;
-  int k = incl - c;
-  while (m) {
-    const int bit = __ffs(m) - 1;
-    m &= m - 1;
-    stage[warp][k++] = (uint32_t)(w * 32 + bit);
-  }
-  __syncwarp();
-  const unsigned long long base = pbase[p] + loc[(g * 4) * P + p];
-  for (int i = lane; i < total; i += 32) {
-    const unsigned long long pos = base + i;
-    if ((int64_t)pos < cap) {
-      pair_node[pos] = stage[warp][i];
-      pair_prim[pos] = (uint32_t)p;
+  unsigned long long base = 0;
+  bool have_base = false;
+#pragma unroll
+  for (int k = 0; k < kEmitGroups; k++) {
+    const int c = __popc(words[k]);
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += t;
     }
+    const int total = __shfl_sync(kFull, incl, 31);
+    if (total == 0) continue;  // warp-uniform
+    if (!have_base) {  // first non-empty group: the tile prefix of the run's first tile
+      base = pbase[p] + loc[(g0 * 4) * P + p];
+      have_base = true;
+    }
+    const int64_t w = (g0 + k) * 32 + lane;
+    uint32_t m = words[k];
+    int j = incl - c;
+    __syncwarp();
+    while (m) {
+      const int bit = __ffs(m) - 1;
+      m &= m - 1;
+      stage[warp][j++] = (uint32_t)(w * 32 + bit);
+    }
+    __syncwarp();
+    for (int i = lane; i < total; i += 32) {
+      const unsigned long long pos = base + i;
+      if ((int64_t)pos < cap) {
+        pair_node[pos] = stage[warp][i];
+        pair_prim[pos] = (uint32_t)p;
+      }
+    }
+    base += total;
   }
 }
 
