@@ -42,12 +42,18 @@ UNIT = "pairs/s"
 # >= 2048 nodes) prep_nodes nn_grid (key-grid ball scan; nn_mask for the quadrotor)
 # nn_prefix scan_totals nn_emit check_pairs (which also restores the node ids)
 KERNELS_PER_STEP = 11
+# states per culling chunk of check_pairs by robot kind (the kernel's
+# Robot<KIND>::CHUNK): unicycle1 0, car1 1, quadrotor 2, quad2d 3
+CHUNK_STATES = {0: 8, 1: 8, 2: 16, 3: 16}
 L2_FLUSH_BYTES = 512 << 20
 
-# DRAM bytes per check_pairs launch from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum), scaled to the full workload by checked pairs; None
-# until a capture exists.
-CHECK_TRAFFIC_PER_PAIR = 79.45e6 / 4126228  # ncu capture of check_pairs, car1_v0 with 50,000 nodes
+# DRAM bytes per checked pair of a check_pairs launch from ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum over the pairs of the captured
+# launch), per workload; scaled to the bench's launch by its checked pairs.
+# Workloads without a capture report traffic null.
+CHECK_TRAFFIC_PER_PAIR = {
+    2: (36.458752e6 + 61.108224e6) / 4126228,  # ncu capture, car1_v0 with 50,000 nodes
+}
 
 
 def parse():
@@ -366,7 +372,7 @@ def run_ours(args, rank, world, local_rank):
     fi = outs["first_invalid"][:n_pairs].cpu().numpy()
     prim = outs["prim"][:n_pairs].cpu().numpy()
     node = outs["node"][:n_pairs].cpu().numpy().view(np.uint32)
-    alg_ops, alg_lower = algorithmic_check_ops(wl, node, verdict, fi, prim)
+    alg_ops, alg_lower = algorithmic_check_ops(wl, node, verdict, fi, prim, chunk=CHUNK_STATES[wl.robot.kind])
     check_s = statistics.mean(check_ms) * 1e-3
     peak = ctypes_peak(lib, dev)
     achieved = alg_ops / check_s / 1e12
@@ -407,7 +413,8 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "roofline": {"bound": "fp32", "kernel": "check_pairs", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": (CHECK_TRAFFIC_PER_PAIR * n_pairs) if CHECK_TRAFFIC_PER_PAIR else None,
+                     "traffic": (CHECK_TRAFFIC_PER_PAIR[args.config] * n_pairs)
+                     if args.config in CHECK_TRAFFIC_PER_PAIR else None,
                      "peak_source": "FMA-chain kernel on this device (dpg_bench_fp32_peak); "
                                     "MEASURED_PEAKS.json holds HBM and bf16 only",
                      "alg_ops_per_launch": alg_ops, "check_ms": 1e3 * check_s,
