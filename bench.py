@@ -393,6 +393,12 @@ def run_ours(args, rank, world, local_rank):
                "sample": f"{n} of {N} frontier states ({cp} checked pairs, {dt:.1f} s)",
                "value_1_thread": rate1, "sample_1_thread": f"{n1} frontier states ({dt1:.1f} s)"}
 
+    # unicycle1 workload: the same expand with the ball radius = delta (alpha 1), the
+    # second reading of the radius the workload's description allows
+    variant = None
+    if args.config == 1:
+        variant = run_radius_variant(args, lib, ctx, wl, x_d, prec, dev)
+
     for h in pinned:
         h.free()
     ctx.close()
@@ -410,6 +416,7 @@ def run_ours(args, rank, world, local_rank):
                    "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",
                    "parallelism": f"replicas x{world}", "wall_ms_per_step": 1e3 * wall / args.steps},
         "e2e": e2e,
+        **({"variant_radius_delta": variant} if variant else {}),
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "roofline": {"bound": "fp32", "kernel": "check_pairs", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak,
@@ -428,6 +435,35 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
     }
     print(json.dumps(line, default=_np_json), flush=True)
+
+
+def run_radius_variant(args, lib, ctx, wl, x_d, prec, dev):
+    """Device-resident expand with radius = delta, timed like the main line."""
+    import torch
+    N, nx = wl.nodes.shape
+    radius = wl.delta
+    n_pairs = ctx.expand(wl.nodes, radius, precision=prec)["n_pairs"]
+    cap = int(n_pairs * 1.02) + 1024
+    outs = {
+        "node": torch.empty(cap, dtype=torch.int32, device=dev),
+        "prim": torch.empty(cap, dtype=torch.int32, device=dev),
+        "verdict": torch.empty(cap, dtype=torch.uint8, device=dev),
+        "first_invalid": torch.empty(cap, dtype=torch.int16, device=dev),
+        "end_state": torch.empty((cap, nx), dtype=torch.float64 if prec == 1 else torch.float32, device=dev),
+        "min_gap": torch.empty(cap, dtype=torch.float32, device=dev),
+        "flags": torch.empty(cap, dtype=torch.uint8, device=dev),
+    }
+    ptrs = {k: v.data_ptr() for k, v in outs.items()}
+    for _ in range(args.warmup):
+        ctx.expand_device(x_d.data_ptr(), N, radius, ptrs, cap, precision=prec)
+    ms, pairs = 0.0, 0
+    for _ in range(args.steps):
+        lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
+        r = ctx.expand_device(x_d.data_ptr(), N, radius, ptrs, cap, precision=prec)
+        ms += sum(ctx.timings()[:4])
+        pairs += r["n_pairs"]
+    return {"radius": radius, "value": pairs / (ms * 1e-3), "unit": UNIT,
+            "checked_pairs_per_step": n_pairs, "ms_per_step": ms / args.steps}
 
 
 def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
@@ -462,9 +498,10 @@ def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
 MLP_IN_USED = 96      # 80 node features + 16 primitive embedding (the rest of the 128 is padding)
 MLP_HIDDEN = 256
 MLP_OUT_USED = 2      # collision logit, cost-to-go
-# assemble, 4 forward GEMMs, loss, 4 x (2 transposes, dW GEMM, column sums,
-# dX GEMM), 9 Adam updates, 4 x (bf16 copy, transpose) + embedding copy
-MLP_KERNELS_PER_TRAIN_STEP = 44
+# assemble, 4 forward GEMMs, loss, 4 x (dW GEMM, dX GEMM), 3 bias-gradient sums, 9 Adam updates,
+# 4 x (bf16 copy, transpose) + embedding copy (the activations' transposes and
+# the bias gradients come from the producing kernels)
+MLP_KERNELS_PER_TRAIN_STEP = 35
 
 
 def mlp_alg_flops(rows):

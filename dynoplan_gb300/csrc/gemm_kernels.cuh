@@ -135,18 +135,23 @@ __host__ __device__ constexpr int tma_stages(int N) {
   return (110 * 1024) / (128 * 128 + N * 128) < 2 ? 2
          : ((110 * 1024) / (128 * 128 + N * 128) > 4 ? 4 : (110 * 1024) / (128 * 128 + N * 128));
 }
-__host__ __device__ constexpr size_t gemm_tma_smem_bytes(int N) {
-  return (size_t)tma_stages(N) * (128 * 128 + N * 128) + 1024 + 256;
+// deeper ring for long K (one CTA per SM): up to 200 KB of stages
+__host__ __device__ constexpr int tma_stages_deep(int N) {
+  return (200 * 1024) / (128 * 128 + N * 128) < 2 ? 2
+         : ((200 * 1024) / (128 * 128 + N * 128) > 6 ? 6 : (200 * 1024) / (128 * 128 + N * 128));
+}
+__host__ __device__ constexpr size_t gemm_tma_smem_bytes(int N, int S) {
+  return (size_t)S * (128 * 128 + N * 128) + 1024 + 256;
 }
 
 constexpr int kTmaThreads = 256;  // 8 warps: all of them drain the accumulator
 
-template <int N, class Epi>
+template <int N, class Epi, int S = tma_stages(N)>
 __global__ void __launch_bounds__(kTmaThreads) gemm_bf16_tma(const __grid_constant__ CUtensorMap tmA,
                                                                const __grid_constant__ CUtensorMap tmB, int M,
                                                                int K, int k_per_split, Epi epi, int *err) {
   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "N");
-  constexpr int S = tma_stages(N);
+  static_assert(S >= 2, "stages");
   constexpr uint32_t kA = 128 * 128, kB = N * 128, kStage = kA + kB;
   extern __shared__ unsigned char smem_raw[];
   const uint32_t raw = umma::smem_u32(smem_raw);
@@ -315,25 +320,41 @@ __device__ __forceinline__ float gelu_grad(float z) {
   return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * du;
 }
 
-// z = acc + bias; keeps z (FP32, for the backward pass) when pre != nullptr;
-// writes gelu(z) in bf16
+// z = acc + bias; keeps gelu'(z) in bf16 for the backward pass when
+// dgelu != nullptr; writes gelu(z) in bf16, and also transposed (actT[col * ldt + row], the
+// K-major operand of the weight-gradient GEMM) when actT != nullptr: the 32
+// lanes of a warp hold 32 consecutive rows, so each column's store is one
+// contiguous 64-byte run
 struct EpiBiasGelu {
   const float *bias;
-  float *pre;
+  __nv_bfloat16 *dgelu;
   __nv_bfloat16 *act;
   int ld;
+  __nv_bfloat16 *actT = nullptr;
+  int64_t ldt = 0;
   __device__ void operator()(int row, int c0, const float *v) const {
     __align__(16) __nv_bfloat16 h[16];
     float z[16];
     load16(bias + c0, z);
 #pragma unroll
     for (int j = 0; j < 16; j++) z[j] += v[j];
-    if (pre) store16(pre + (int64_t)row * ld + c0, z);
+    if (dgelu) {
+      __align__(16) __nv_bfloat16 d[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) d[j] = __float2bfloat16_rn(gelu_grad(z[j]));
+      uint4 *gd = reinterpret_cast<uint4 *>(dgelu + (int64_t)row * ld + c0);
+      gd[0] = reinterpret_cast<const uint4 *>(d)[0];
+      gd[1] = reinterpret_cast<const uint4 *>(d)[1];
+    }
 #pragma unroll
     for (int j = 0; j < 16; j++) h[j] = __float2bfloat16_rn(gelu(z[j]));
     uint4 *dst = reinterpret_cast<uint4 *>(act + (int64_t)row * ld + c0);
     dst[0] = reinterpret_cast<const uint4 *>(h)[0];
     dst[1] = reinterpret_cast<const uint4 *>(h)[1];
+    if (actT) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) actT[(int64_t)(c0 + j) * ldt + row] = h[j];
+    }
   }
 };
 // out = acc + bias (FP32), first n_valid columns

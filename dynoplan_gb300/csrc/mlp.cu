@@ -2,6 +2,8 @@
 // surrogate MLP built on it.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <cstring>
 #include <string>
 
@@ -53,8 +55,21 @@ cudaError_t launch_gemm_n(const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M,
   dim3 grid((M + 127) / 128, (K + per - 1) / per);
   CUtensorMap ta, tb;
   if (tma && make_kmajor_map(&ta, A, (uint64_t)M, (uint64_t)K, 128) && make_kmajor_map(&tb, B, N, (uint64_t)K, N)) {
-    auto kern = gemm_bf16_tma<N, Epi>;
-    const size_t sm = gemm_tma_smem_bytes(N);
+    // long K per CTA (the split-K weight gradients): the deep ring, one CTA per SM
+    if constexpr (std::is_same<Epi, EpiAtomicF32>::value) {
+      if (per >= 8 * kGemmKChunk) {
+        constexpr int S = tma_stages_deep(N);
+        auto kern = gemm_bf16_tma<N, Epi, S>;
+        const size_t sm = gemm_tma_smem_bytes(N, S);
+        static cudaError_t attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (attr != cudaSuccess) return attr;
+        kern<<<grid, kTmaThreads, sm, st>>>(ta, tb, M, K, per, epi, err);
+        return cudaGetLastError();
+      }
+    }
+    constexpr int S = tma_stages(N);
+    auto kern = gemm_bf16_tma<N, Epi, S>;
+    const size_t sm = gemm_tma_smem_bytes(N, S);
     static cudaError_t attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (attr != cudaSuccess) return attr;
     kern<<<grid, kTmaThreads, sm, st>>>(ta, tb, M, K, per, epi, err);
@@ -139,7 +154,13 @@ struct dpg_mlp {
   // activations and backward buffers (rows_pad rows)
   __nv_bfloat16 *X = nullptr, *H[3] = {}, *dZa = nullptr, *dZb = nullptr, *dY = nullptr, *T1 = nullptr,
                 *T2 = nullptr;
-  float *Z[3] = {}, *out = nullptr, *loss = nullptr;
+  // training: the activations and loss gradient transposed ([cols x rows_pad],
+  // the K-major operands of the weight-gradient GEMMs), written by the
+  // producing kernels; T2 holds X^T, T1 the current layer's dZ^T
+  __nv_bfloat16 *HT[3] = {}, *dYT = nullptr;
+  float *dpart = nullptr;  // per-warp partial bias gradients [rows_pad / 32 x 256]
+  __nv_bfloat16 *G[3] = {};  // gelu'(pre-activation) of layers 1-3 (training)
+  float *out = nullptr, *loss = nullptr;
   int *err = nullptr;
   int step = 0;
   int fused = 1;  // forward through mlp_forward_fused when the tensor maps can be made
@@ -205,13 +226,14 @@ template <class T> cudaError_t dalloc(T **p, size_t count) {
   return cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(count, 1));
 }
 
-// forward of rows [0, B) of the assembled X; keeps Z (FP32) when train
+// forward of rows [0, B) of the assembled X; keeps gelu'(Z) (bf16) and the
+// activations transposed (HT) when train
 cudaError_t forward_rows(dpg_mlp *M, int64_t B, bool train, float *out, cudaStream_t st) {
   const int64_t Bp = pad128(B);
   cudaError_t e;
   const __nv_bfloat16 *in = M->X;
   for (int l = 0; l < 3; l++) {
-    EpiBiasGelu epi{M->w[2 * l + 1], train ? M->Z[l] : nullptr, M->H[l], kMlpHidden};
+    EpiBiasGelu epi{M->w[2 * l + 1], train ? M->G[l] : nullptr, M->H[l], kMlpHidden, train ? M->HT[l] : nullptr, Bp};
     e = launch_gemm(kMlpHidden, in, M->W16[l], (int)Bp, kIn[l], 1, epi, M->err, st);
     if (e != cudaSuccess) return e;
     in = M->H[l];
@@ -265,7 +287,10 @@ int dpg_mlp_create(dpg_mlp **out, int device, int n_prims, int64_t max_rows, uin
        dalloc(&M->out, (size_t)R * 2) == cudaSuccess && dalloc(&M->loss, 1) == cudaSuccess &&
        dalloc(&M->err, 1) == cudaSuccess;
   for (int l = 0; l < 3 && ok; l++)
-    ok = dalloc(&M->H[l], (size_t)R * kMlpHidden) == cudaSuccess && dalloc(&M->Z[l], (size_t)R * kMlpHidden) == cudaSuccess;
+    ok = dalloc(&M->H[l], (size_t)R * kMlpHidden) == cudaSuccess && dalloc(&M->G[l], (size_t)R * kMlpHidden) == cudaSuccess &&
+         dalloc(&M->HT[l], (size_t)R * kMlpHidden) == cudaSuccess;
+  ok = ok && dalloc(&M->dYT, (size_t)R * kMlpOutPad) == cudaSuccess &&
+       dalloc(&M->dpart, (size_t)(R / 32) * kMlpHidden) == cudaSuccess;
   ok = ok && cudaEventCreate(&M->e0) == cudaSuccess && cudaEventCreate(&M->e1) == cudaSuccess;
   ok = ok && dalloc(&M->in_node, R) == cudaSuccess && dalloc(&M->in_prim, R) == cudaSuccess &&
        dalloc(&M->in_target, 2 * R) == cudaSuccess && dalloc(&M->hp, 4) == cudaSuccess &&
@@ -315,8 +340,11 @@ void dpg_mlp_destroy(dpg_mlp *M) {
   }
   for (int l = 0; l < 3; l++) {
     cudaFree(M->H[l]);
-    cudaFree(M->Z[l]);
+    cudaFree(M->G[l]);
+    cudaFree(M->HT[l]);
   }
+  cudaFree(M->dYT);
+  cudaFree(M->dpart);
   void *bufs[] = {M->emb16, M->X,   M->dZa,     M->dZb,     M->dY,     M->T1,  M->T2,
                   M->out,   M->loss, M->err, M->in_node, M->in_prim, M->in_target, M->hp};
   for (void *b : bufs) cudaFree(b);
@@ -381,7 +409,7 @@ int dpg_mlp_forward(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_
     const int64_t B = std::min(M->max_rows, n - r0), Bp = pad128(B);
     const int64_t chunks = Bp * (kMlpIn / 8);
     mlp_assemble<<<(unsigned)((chunks + 255) / 256), 256, 0, st>>>(nf, M->emb16, node_dev + r0, prim_dev + r0, B, Bp,
-                                                                    M->X);
+                                                                    M->X, nullptr);
     if (forward_rows(M, B, false, out_dev + 2 * r0, st) != cudaSuccess) return DPG_ERR_CUDA;
     flops += forward_flops(Bp);
   }
@@ -400,45 +428,44 @@ int dpg_mlp_forward(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_
 // fixed input buffers and the hyper-parameters from M->hp (capturable).
 static cudaError_t enqueue_train(dpg_mlp *M, const __nv_bfloat16 *nf, int64_t B, cudaStream_t st) {
   const int64_t Bp = pad128(B);
-  const int split = (int)std::max<int64_t>(1, std::min<int64_t>(64, Bp / 1024));
+  // split-K of the weight-gradient GEMMs (K = the batch): about one CTA per SM
+  auto split_for = [&](int rows) {
+    const int tiles = (rows + 127) / 128;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(std::max(M->sm_count, 1) / tiles, Bp / 512));
+  };
   cudaMemsetAsync(M->err, 0, sizeof(int), st);
   cudaMemsetAsync(M->loss, 0, sizeof(float), st);
   for (int i = 0; i < DPG_MLP_NPARAM; i++) cudaMemsetAsync(M->g[i], 0, sizeof(float) * M->n[i], st);
   const int64_t chunks = Bp * (kMlpIn / 8);
-  mlp_assemble<<<(unsigned)((chunks + 255) / 256), 256, 0, st>>>(nf, M->emb16, M->in_node, M->in_prim, B, Bp, M->X);
+  mlp_assemble<<<(unsigned)((chunks + 255) / 256), 256, 0, st>>>(nf, M->emb16, M->in_node, M->in_prim, B, Bp, M->X,
+                                                                  M->T2);
   cudaError_t e = forward_rows(M, B, true, M->out, st);
   if (e != cudaSuccess) return e;
-  mlp_loss<<<(unsigned)((Bp + 255) / 256), 256, 0, st>>>(M->out, M->in_target, B, Bp, M->hp, M->dY, M->loss);
-  dim3 tb(32, 8);
-  auto transpose = [&](const __nv_bfloat16 *in, __nv_bfloat16 *o, int64_t rows, int64_t cols) {
-    dim3 tg((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
-    transpose_bf16<<<tg, tb, 0, st>>>(in, o, rows, cols);
+  mlp_loss<<<(unsigned)((Bp + 255) / 256), 256, 0, st>>>(M->out, M->in_target, B, Bp, M->hp, M->dY, M->loss, M->dYT,
+                                                          M->g[DPG_MLP_B4]);
+  // the transposed operands and the bias gradients come from the kernels that
+  // produce the activations and dZ (Bp is a multiple of 128: whole warps of rows)
+  auto bias_grad = [&](int which) {  // the partial column sums of the last dZ into g[which]
+    sum_rows_f32<<<kMlpHidden / 32, 256, 0, st>>>(M->dpart, Bp / 32, kMlpHidden, kMlpHidden, M->g[which]);
   };
-  auto colsum = [&](const __nv_bfloat16 *in, int ld, int ncol, float *o) {
-    dim3 g((ncol + 31) / 32, 64), b(32, 8);
-    column_sums_bf16<<<g, b, 0, st>>>(in, Bp, ld, ncol, o);
-  };
-  // layer 4: dW4 = dY^T H3 (16 rows), db4, dZ3 = (dY W4) * gelu'(Z3)
-  transpose(M->dY, M->T1, Bp, kDY);
-  transpose(M->H[2], M->T2, Bp, kMlpHidden);
-  e = launch_gemm(kMlpHidden, M->T1, M->T2, kMlpOutPad, (int)Bp, split,
+  // layer 4: dW4 = dY^T H3 (16 rows), dZ3 = (dY W4) * gelu'(Z3) with dZ3^T and db3
+  e = launch_gemm(kMlpHidden, M->dYT, M->HT[2], kMlpOutPad, (int)Bp, split_for(kMlpOutPad),
                   EpiAtomicF32{M->g[DPG_MLP_W4], kMlpHidden, kMlpHidden}, M->err, st);
-  colsum(M->dY, kDY, kMlpOutPad, M->g[DPG_MLP_B4]);
   if (e == cudaSuccess)
-    e = launch_gemm(kMlpHidden, M->dY, M->WT16[3], (int)Bp, kDY, 1, EpiGeluGrad{M->Z[2], M->dZa, kMlpHidden},
-                    M->err, st);
+    e = launch_gemm(kMlpHidden, M->dY, M->WT16[3], (int)Bp, kDY, 1,
+                    EpiGeluGrad{M->G[2], M->dZa, kMlpHidden, M->T1, Bp, M->dpart}, M->err, st);
+  if (e == cudaSuccess) bias_grad(DPG_MLP_B3);
   __nv_bfloat16 *dz = M->dZa, *dz_next = M->dZb;
-  for (int l = 2; l >= 0 && e == cudaSuccess; l--) {  // layers 3, 2, 1
-    const __nv_bfloat16 *h_in = l > 0 ? M->H[l - 1] : M->X;
-    transpose(dz, M->T1, Bp, kMlpHidden);
-    transpose(h_in, M->T2, Bp, kIn[l]);
-    e = launch_gemm(kIn[l], M->T1, M->T2, kMlpHidden, (int)Bp, split,
-                    EpiAtomicF32{M->g[2 * l], kIn[l], kIn[l]}, M->err, st);
-    colsum(dz, kMlpHidden, kMlpHidden, M->g[2 * l + 1]);
+  for (int l = 2; l >= 0 && e == cudaSuccess; l--) {  // layers 3, 2, 1: dZ^T in T1
+    const __nv_bfloat16 *h_inT = l > 0 ? M->HT[l - 1] : M->T2;
+    e = launch_gemm(kIn[l], M->T1, h_inT, kMlpHidden, (int)Bp, split_for(kMlpHidden),
+                    EpiAtomicF32{M->g[2 * l], kIn[l], kIn[l]},
+                    M->err, st);
     if (e != cudaSuccess) break;
     if (l > 0)
       e = launch_gemm(kMlpHidden, dz, M->WT16[l], (int)Bp, kMlpHidden, 1,
-                      EpiGeluGrad{M->Z[l - 1], dz_next, kMlpHidden}, M->err, st);
+                      EpiGeluGrad{M->G[l - 1], dz_next, kMlpHidden, M->T1, Bp, M->dpart}, M->err, st);
+    if (e == cudaSuccess && l > 0) bias_grad(2 * (l - 1) + 1);
     else
       // only the embedding columns 80..95 of dX are needed: rows 80..95 of W1^T
       e = launch_gemm(kMlpEmb, dz, M->WT16[0] + (size_t)kMlpNodeFeat * kMlpHidden, (int)Bp, kMlpHidden, 1,

@@ -83,12 +83,16 @@ __global__ void mlp_node_features(NodeView nv, EnvView ev, GoalView gv, __nv_bfl
 }
 
 // X[b] = [node_feat[node[b]] | emb[prim[b]]], one thread per 16-byte chunk
+// Thread per (8-column chunk c, row b), rows fastest; when XT is set the
+// rows are also written transposed (XT[col * B_pad + b]: consecutive threads
+// store consecutive rows of a column).
 static __global__ void mlp_assemble(const __nv_bfloat16 *node_feat, const __nv_bfloat16 *emb, const uint32_t *node,
-                             const uint32_t *prim, int64_t B, int64_t B_pad, __nv_bfloat16 *X) {
+                             const uint32_t *prim, int64_t B, int64_t B_pad, __nv_bfloat16 *X,
+                             __nv_bfloat16 *XT) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t b = i / (kMlpIn / 8);
-  const int c = (int)(i % (kMlpIn / 8));
-  if (b >= B_pad) return;
+  const int c = (int)(i / B_pad);
+  const int64_t b = i - (int64_t)c * B_pad;
+  if (c >= kMlpIn / 8) return;
   uint4 v = make_uint4(0, 0, 0, 0);
   if (b < B) {
     if (c < kMlpNodeFeat / 8)
@@ -97,6 +101,11 @@ static __global__ void mlp_assemble(const __nv_bfloat16 *node_feat, const __nv_b
       v = reinterpret_cast<const uint4 *>(emb + (int64_t)prim[b] * kMlpEmb)[c - kMlpNodeFeat / 8];
   }
   reinterpret_cast<uint4 *>(X + b * kMlpIn)[c] = v;
+  if (XT) {
+    const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) XT[(int64_t)(8 * c + j) * B_pad + b] = h[j];
+  }
 }
 
 __device__ __forceinline__ float softplus(float x) { return x > 20.f ? x : log1pf(__expf(x)); }
@@ -106,11 +115,14 @@ __device__ __forceinline__ float sigmoid(float x) { return 1.f / (1.f + __expf(-
 // columns >= 2 zero) = d loss / d [l, c]; loss accumulated into *loss_sum
 // (ctg_weight = hp[1]: the step's hyper-parameters live in device memory so a
 // captured training step can be replayed with new values)
+// When dYT is set, also the first kMlpOutPad columns of dY transposed
+// (dYT[j * B_pad + b]) and the head's bias gradient (column sums of the bf16
+// dY, two non-zero columns) added into db.
 static __global__ void mlp_loss(const float *out, const float *target, int64_t B, int64_t B_pad, const float *hp,
-                         __nv_bfloat16 *dY, float *loss_sum) {
+                         __nv_bfloat16 *dY, float *loss_sum, __nv_bfloat16 *dYT, float *db) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const float ctg_weight = hp[1];
-  float l = 0.f;
+  float l = 0.f, g0 = 0.f, g1 = 0.f;
   if (b < B_pad) {
     __align__(16) __nv_bfloat16 row[64];
 #pragma unroll
@@ -131,25 +143,66 @@ static __global__ void mlp_loss(const float *out, const float *target, int64_t B
     uint4 *dst = reinterpret_cast<uint4 *>(dY + b * 64);
 #pragma unroll
     for (int j = 0; j < 8; j++) dst[j] = reinterpret_cast<const uint4 *>(row)[j];
+    if (dYT) {
+#pragma unroll
+      for (int j = 0; j < kMlpOutPad; j++) dYT[j * B_pad + b] = row[j];
+    }
+    g0 = __bfloat162float(row[0]);
+    g1 = __bfloat162float(row[1]);
   }
-  for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
-  if ((threadIdx.x & 31) == 0 && l != 0.f) atomicAdd(loss_sum, l);
+  for (int o = 16; o > 0; o >>= 1) {
+    l += __shfl_down_sync(0xffffffffu, l, o);
+    g0 += __shfl_down_sync(0xffffffffu, g0, o);
+    g1 += __shfl_down_sync(0xffffffffu, g1, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (l != 0.f) atomicAdd(loss_sum, l);
+    if (db && g0 != 0.f) atomicAdd(db, g0);
+    if (db && g1 != 0.f) atomicAdd(db + 1, g1);
+  }
 }
 
-// dZ = dH * gelu'(Z): the epilogue of dH = dZnext * W
+// dZ = dH * gelu'(Z) (gelu' kept in bf16 by the forward epilogue): the
+// epilogue of dH = dZnext * W.  Optionally also
+// dZ transposed (dzT[col * ldt + row], the K-major operand of the
+// weight-gradient GEMM) and partial bias gradients: the column sums of the
+// bf16 dZ over each warp's 32 rows, stored (no atomics) at row
+// 4 blockIdx.x + (warp % 4) of dpart [M / 32 x ld], summed by sum_rows_f32.
+// The partial sums need whole warps of rows: M a multiple of 128.
 struct EpiGeluGrad {
-  const float *pre;
+  const __nv_bfloat16 *dgelu;
   __nv_bfloat16 *dz;
   int ld;
+  __nv_bfloat16 *dzT = nullptr;
+  int64_t ldt = 0;
+  float *dpart = nullptr;
   __device__ void operator()(int row, int c0, const float *v) const {
-    __align__(16) __nv_bfloat16 h[16];
-    float z[16];
-    load16(pre + (int64_t)row * ld + c0, z);
+    __align__(16) __nv_bfloat16 h[16], d[16];
+    const uint4 *gd = reinterpret_cast<const uint4 *>(dgelu + (int64_t)row * ld + c0);
+    reinterpret_cast<uint4 *>(d)[0] = gd[0];
+    reinterpret_cast<uint4 *>(d)[1] = gd[1];
 #pragma unroll
-    for (int j = 0; j < 16; j++) h[j] = __float2bfloat16_rn(v[j] * gelu_grad(z[j]));
+    for (int j = 0; j < 16; j++) h[j] = __float2bfloat16_rn(v[j] * __bfloat162float(d[j]));
     uint4 *dst = reinterpret_cast<uint4 *>(dz + (int64_t)row * ld + c0);
     dst[0] = reinterpret_cast<const uint4 *>(h)[0];
     dst[1] = reinterpret_cast<const uint4 *>(h)[1];
+    if (dzT) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) dzT[(int64_t)(c0 + j) * ldt + row] = h[j];
+    }
+    if (dpart) {
+      float *prow = dpart + ((int64_t)blockIdx.x * 4 + ((threadIdx.x >> 5) & 3)) * ld + c0;
+      const int lane = threadIdx.x & 31;
+      float mine = 0.f;  // lane j < 16 keeps column c0 + j
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        float t = __bfloat162float(h[j]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == j) mine = t;
+      }
+      if (lane < 16) prow[lane] = mine;
+    }
   }
 };
 
@@ -182,20 +235,21 @@ static __global__ void transpose_bf16(const __nv_bfloat16 *in, __nv_bfloat16 *ou
   }
 }
 
-// out[j] = sum_b in[b * ld + j] for j < n (bias gradients), block per column group
-static __global__ void column_sums_bf16(const __nv_bfloat16 *in, int64_t B, int ld, int n, float *out) {
-  const int j = blockIdx.x * 32 + threadIdx.x;
+// out[j] += sum_r part[r * ld + j] for j < n: block = 32 columns x 8 row segments
+static __global__ void __launch_bounds__(256) sum_rows_f32(const float *part, int64_t rows, int ld, int n,
+                                                           float *out) {
+  __shared__ float red[8][33];
+  const int j = blockIdx.x * 32 + (threadIdx.x & 31), sg = threadIdx.x >> 5;
   float s = 0.f;
   if (j < n)
-    for (int64_t b = blockIdx.y * blockDim.y + threadIdx.y; b < B; b += (int64_t)gridDim.y * blockDim.y)
-      s += __bfloat162float(in[b * ld + j]);
-  __shared__ float red[8][33];
-  red[threadIdx.y][threadIdx.x] = s;
+    for (int64_t r = sg; r < rows; r += 8) s += part[r * ld + j];
+  red[sg][threadIdx.x & 31] = s;
   __syncthreads();
-  if (threadIdx.y == 0 && j < n) {
+  if (sg == 0 && j < n) {
     float t = 0.f;
-    for (int i = 0; i < blockDim.y; i++) t += red[i][threadIdx.x];
-    atomicAdd(out + j, t);
+#pragma unroll
+    for (int k = 0; k < 8; k++) t += red[k][threadIdx.x];
+    out[j] += t;
   }
 }
 
