@@ -498,10 +498,10 @@ def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
 MLP_IN_USED = 96      # 80 node features + 16 primitive embedding (the rest of the 128 is padding)
 MLP_HIDDEN = 256
 MLP_OUT_USED = 2      # collision logit, cost-to-go
-# assemble, 4 forward GEMMs, loss, 4 x (dW GEMM, dX GEMM), 3 bias-gradient sums, 9 Adam updates,
-# 4 x (bf16 copy, transpose) + embedding copy (the activations' transposes and
-# the bias gradients come from the producing kernels)
-MLP_KERNELS_PER_TRAIN_STEP = 35
+# assemble, 4 forward GEMMs, loss, 4 x (dW GEMM, dX GEMM), 3 bias-gradient sums,
+# one Adam launch over every parameter (also the bf16 and transposed copies);
+# the activations' transposes and bias gradients come from the producing kernels
+MLP_KERNELS_PER_TRAIN_STEP = 18
 
 
 def mlp_alg_flops(rows):

@@ -446,7 +446,7 @@ static cudaError_t enqueue_train(dpg_mlp *M, const __nv_bfloat16 *nf, int64_t B,
   // the transposed operands and the bias gradients come from the kernels that
   // produce the activations and dZ (Bp is a multiple of 128: whole warps of rows)
   auto bias_grad = [&](int which) {  // the partial column sums of the last dZ into g[which]
-    sum_rows_f32<<<kMlpHidden / 32, 256, 0, st>>>(M->dpart, Bp / 32, kMlpHidden, kMlpHidden, M->g[which]);
+    sum_rows_f32<<<dim3(kMlpHidden / 32, 32), 256, 0, st>>>(M->dpart, Bp / 32, kMlpHidden, kMlpHidden, M->g[which]);
   };
   // layer 4: dW4 = dY^T H3 (16 rows), dZ3 = (dY W4) * gelu'(Z3) with dZ3^T and db3
   e = launch_gemm(kMlpHidden, M->dYT, M->HT[2], kMlpOutPad, (int)Bp, split_for(kMlpOutPad),
@@ -473,13 +473,24 @@ static cudaError_t enqueue_train(dpg_mlp *M, const __nv_bfloat16 *nf, int64_t B,
     std::swap(dz, dz_next);
   }
   if (e != cudaSuccess) return e;
-  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;  // Adam
+  // Adam on every parameter and the bf16 operand copies, one launch
+  static_assert(kAdamSegs == DPG_MLP_NPARAM, "one Adam segment per parameter");
+  AdamArgs aa{};
   for (int i = 0; i < DPG_MLP_NPARAM; i++) {
-    const int64_t n = M->n[i];
-    adam_update<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(M->w[i], M->g[i], M->m[i], M->v[i], n, M->hp, b1, b2,
-                                                             eps, nullptr, nullptr, 0, 1);
-    refresh_bf16(M, i, st);
+    AdamSeg &q = aa.seg[i];
+    q = AdamSeg{M->w[i], M->m[i], M->v[i], M->g[i], nullptr, nullptr, 1, 1};
+    if (i == DPG_MLP_EMB) {
+      q.w16 = M->emb16;
+    } else if (i % 2 == 0) {  // weights [out x in]: bf16 copy and its transpose
+      const int l = i / 2;
+      q.w16 = M->W16[l];
+      q.wT = M->WT16[l];
+      q.cols = kIn[l];
+      q.ldT = l < 3 ? kOut[l] : kDY;  // layer 4: [256 x 64] rows, columns >= 16 stay zero
+    }
+    aa.start[i + 1] = aa.start[i] + M->n[i];
   }
+  adam_all<<<(unsigned)((aa.start[DPG_MLP_NPARAM] + 255) / 256), 256, 0, st>>>(aa, M->hp, 0.9f, 0.999f, 1e-8f);
   return cudaGetLastError();
 }
 

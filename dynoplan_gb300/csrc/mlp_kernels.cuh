@@ -235,40 +235,60 @@ static __global__ void transpose_bf16(const __nv_bfloat16 *in, __nv_bfloat16 *ou
   }
 }
 
-// out[j] += sum_r part[r * ld + j] for j < n: block = 32 columns x 8 row segments
+// out[j] += sum_r part[r * ld + j] for j < n.  Block = 32 columns x 8 warps;
+// gridDim.y splits the rows; one atomic per (block, column).
 static __global__ void __launch_bounds__(256) sum_rows_f32(const float *part, int64_t rows, int ld, int n,
                                                            float *out) {
   __shared__ float red[8][33];
   const int j = blockIdx.x * 32 + (threadIdx.x & 31), sg = threadIdx.x >> 5;
+  const int64_t per = (rows + gridDim.y - 1) / gridDim.y;
+  const int64_t r0 = blockIdx.y * per, r1 = min(rows, r0 + per);
   float s = 0.f;
-  if (j < n)
-    for (int64_t r = sg; r < rows; r += 8) s += part[r * ld + j];
+  if (j < n) {
+#pragma unroll 4
+    for (int64_t r = r0 + sg; r < r1; r += 8) s += part[r * ld + j];
+  }
   red[sg][threadIdx.x & 31] = s;
   __syncthreads();
   if (sg == 0 && j < n) {
     float t = 0.f;
 #pragma unroll
     for (int k = 0; k < 8; k++) t += red[k][threadIdx.x];
-    out[j] += t;
+    atomicAdd(out + j, t);
   }
 }
 
-// Adam on FP32 master weights; writes the bf16 copy (and, if wT, its
-// transpose of a rows x cols matrix).  hp = [lr, ctg_weight, 1 - b1^t, 1 - b2^t]
-static __global__ void adam_update(float *w, const float *g, float *m, float *v, int64_t n, const float *hp, float b1,
-                            float b2, float eps, __nv_bfloat16 *w16, __nv_bfloat16 *wT, int rows, int cols) {
+// Adam over every parameter in one launch: segment s is elements
+// [start[s], start[s + 1]) of the concatenation; the bf16 copy (w16) and the
+// transposed bf16 copy (wT[(k % cols) * ldT + k / cols]) are written when set.
+struct AdamSeg {
+  float *w, *m, *v;
+  const float *g;
+  __nv_bfloat16 *w16, *wT;
+  int cols, ldT;
+};
+constexpr int kAdamSegs = 9;
+struct AdamArgs {
+  AdamSeg seg[kAdamSegs];
+  int64_t start[kAdamSegs + 1];
+};
+static __global__ void adam_all(AdamArgs a, const float *hp, float b1, float b2, float eps) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= a.start[kAdamSegs]) return;
+  int s = 0;
+  while (s + 1 < kAdamSegs && i >= a.start[s + 1]) s++;
+  const AdamSeg &q = a.seg[s];
+  const int64_t k = i - a.start[s];
   const float lr = hp[0], bc1 = hp[2], bc2 = hp[3];
-  const float gi = g[i];
-  const float mi = b1 * m[i] + (1.f - b1) * gi;
-  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-  m[i] = mi;
-  v[i] = vi;
-  const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
-  w[i] = wi;
-  if (w16) w16[i] = __float2bfloat16_rn(wi);
-  if (wT) wT[(int64_t)(i % cols) * rows + i / cols] = __float2bfloat16_rn(wi);
+  const float gi = q.g[k];
+  const float mi = b1 * q.m[k] + (1.f - b1) * gi;
+  const float vi = b2 * q.v[k] + (1.f - b2) * gi * gi;
+  q.m[k] = mi;
+  q.v[k] = vi;
+  const float wi = q.w[k] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  q.w[k] = wi;
+  if (q.w16) q.w16[k] = __float2bfloat16_rn(wi);
+  if (q.wT) q.wT[(k % q.cols) * q.ldT + k / q.cols] = __float2bfloat16_rn(wi);
 }
 
 static __global__ void f32_to_bf16(const float *in, __nv_bfloat16 *out, int64_t n) {
