@@ -320,11 +320,44 @@ __device__ __forceinline__ float gelu_grad(float z) {
   return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * du;
 }
 
+// Transposed store of a warp's 32 rows x 16 columns of bf16 (lane = row,
+// h = the lane's 16 values of columns c0..c0+15): staged in shared memory,
+// then written as 16-byte runs, dst[(c0 + c) * ldt + row0 + r] for the warp's
+// first row row0.  With colsum set, lanes c < 16 also write the sum over the
+// 32 rows of column c0 + c to colsum[c].  All 32 lanes must call it (M a
+// multiple of 32); row0 and ldt multiples of 8.
+__device__ __forceinline__ void store_transposed16(__nv_bfloat16 *dst, int64_t ldt, int row, int c0,
+                                                   const __nv_bfloat16 *h, float *colsum = nullptr) {
+  __shared__ __align__(16) __nv_bfloat16 tbuf[kTmaThreads / 32][16][40];  // 80-byte rows
+  const int w = (threadIdx.x >> 5) % (kTmaThreads / 32), lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < 16; j++) tbuf[w][j][lane] = h[j];
+  __syncwarp();
+  const int row0 = row - lane;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int q = lane + 32 * k, c = q >> 2, part = q & 3;  // column c, rows 8 part .. 8 part + 7
+    const uint4 val = *reinterpret_cast<const uint4 *>(&tbuf[w][c][8 * part]);
+    *reinterpret_cast<uint4 *>(dst + (int64_t)(c0 + c) * ldt + row0 + 8 * part) = val;
+  }
+  if (colsum && lane < 16) {
+    float t = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint4 val = *reinterpret_cast<const uint4 *>(&tbuf[w][lane][8 * k]);
+      const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&val);
+#pragma unroll
+      for (int i = 0; i < 8; i++) t += __bfloat162float(e[i]);
+    }
+    colsum[lane] = t;
+  }
+  __syncwarp();
+}
+
 // z = acc + bias; keeps gelu'(z) in bf16 for the backward pass when
-// dgelu != nullptr; writes gelu(z) in bf16, and also transposed (actT[col * ldt + row], the
-// K-major operand of the weight-gradient GEMM) when actT != nullptr: the 32
-// lanes of a warp hold 32 consecutive rows, so each column's store is one
-// contiguous 64-byte run
+// dgelu != nullptr; writes gelu(z) in bf16, and also transposed (actT[col *
+// ldt + row], the K-major operand of the weight-gradient GEMM) when actT !=
+// nullptr (M a multiple of 32)
 struct EpiBiasGelu {
   const float *bias;
   __nv_bfloat16 *dgelu;
@@ -351,10 +384,7 @@ struct EpiBiasGelu {
     uint4 *dst = reinterpret_cast<uint4 *>(act + (int64_t)row * ld + c0);
     dst[0] = reinterpret_cast<const uint4 *>(h)[0];
     dst[1] = reinterpret_cast<const uint4 *>(h)[1];
-    if (actT) {
-#pragma unroll
-      for (int j = 0; j < 16; j++) actT[(int64_t)(c0 + j) * ldt + row] = h[j];
-    }
+    if (actT) store_transposed16(actT, ldt, row, c0, h);
   }
 };
 // out = acc + bias (FP32), first n_valid columns

@@ -186,12 +186,10 @@ struct EpiGeluGrad {
     uint4 *dst = reinterpret_cast<uint4 *>(dz + (int64_t)row * ld + c0);
     dst[0] = reinterpret_cast<const uint4 *>(h)[0];
     dst[1] = reinterpret_cast<const uint4 *>(h)[1];
-    if (dzT) {
-#pragma unroll
-      for (int j = 0; j < 16; j++) dzT[(int64_t)(c0 + j) * ldt + row] = h[j];
-    }
-    if (dpart) {
-      float *prow = dpart + ((int64_t)blockIdx.x * 4 + ((threadIdx.x >> 5) & 3)) * ld + c0;
+    float *prow = dpart ? dpart + ((int64_t)blockIdx.x * 4 + ((threadIdx.x >> 5) & 3)) * ld + c0 : nullptr;
+    if (dzT) {  // the transposed store also sums the staged columns
+      store_transposed16(dzT, ldt, row, c0, h, prow);
+    } else if (prow) {
       const int lane = threadIdx.x & 31;
       float mine = 0.f;  // lane j < 16 keeps column c0 + j
 #pragma unroll
