@@ -64,6 +64,3 @@ struct dpg_ctx {
   double timings[4] = {0, 0, 0, 0};
 };
 
-// canonical FP64 state rows of the uploaded primitives ([S][nx], the device
-// table after the canonical rollout), copied to the host on first use
-int dpg_ctx_host_states(dpg_ctx *c, std::vector<double> &out);

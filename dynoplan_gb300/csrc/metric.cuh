@@ -15,7 +15,7 @@ template <int KIND>
 __device__ float full_dist32(const float4 w, const float *a, const float *b) {
   auto so2f = [](float x, float y) {
     float d = fabsf(x - y);
-    d = fmodf(d, 6.2831853071795865f);
+    if (d >= 6.2831853071795865f) d = fmodf(d, 6.2831853071795865f);
     return d > 3.1415926535897932f ? 6.2831853071795865f - d : d;
   };
   if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
@@ -37,7 +37,7 @@ template <int KIND>
 __device__ double full_dist64(const RobotParams &rp, const double *a, const double *b) {
   auto so2d = [](double x, double y) {
     double d = fabs(x - y);
-    d = fmod(d, kTwoPi);
+    if (d >= kTwoPi) d = fmod(d, kTwoPi);
     return d > kPi ? kTwoPi - d : d;
   };
   if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {

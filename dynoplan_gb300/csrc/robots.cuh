@@ -82,7 +82,7 @@ constexpr double kTwoPi = 6.283185307179586476925286766559;
 // wrapped angle distance, FP64, the oracle's formula (fabs, fmod, reflect)
 __device__ __forceinline__ double so2_dist64(double a, double b) {
   double d = fabs(a - b);
-  d = fmod(d, kTwoPi);
+  if (d >= kTwoPi) d = fmod(d, kTwoPi);  // (fmod(d, 2 pi) = d below 2 pi)
   return d > kPi ? kTwoPi - d : d;
 }
 

@@ -27,7 +27,7 @@ constexpr double kPiH = 3.1415926535897932384626433832795;
 
 double so2(double a, double b) {
   double d = std::fabs(a - b);
-  d = std::fmod(d, kTwoPiH);
+  if (d >= kTwoPiH) d = std::fmod(d, kTwoPiH);  // (fmod(d, 2 pi) = d below 2 pi)
   return d > kPiH ? kTwoPiH - d : d;
 }
 double n3(double a, double b, double c) { return std::sqrt(a * a + b * b + c * c); }
@@ -72,32 +72,50 @@ double lower_bound_time(const dpg_robot_desc &r, const double *a, const double *
   }
 }
 
-// components shifted by the node offset: positions, then velocities
-int offset_comps(int kind, int *pos, int *vel) {
-  switch (kind) {
-    case DPG_ROBOT_QUAD2D: pos[0] = 0; pos[1] = 1; vel[0] = 3; vel[1] = 4; return 2;
-    case DPG_ROBOT_QUAD3D:
-      pos[0] = 0; pos[1] = 1; pos[2] = 2; vel[0] = 7; vel[1] = 8; vel[2] = 9; return 3;
-    default: pos[0] = 0; pos[1] = 1; return 2;
+// the host `lower_bound_time` (max over blocks of distance / max speed)
+template <int KIND>
+__device__ double lbt_exact(const double *a, const double *b) {
+  auto mx = [](double x, double y) { return x < y ? y : x; };  // std::max
+  if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
+    return mx(hypot(a[0] - b[0], a[1] - b[1]) / 0.5, so2_dist64(a[2], b[2]) / 0.5);
+  } else if constexpr (KIND == DPG_ROBOT_CAR1) {
+    return mx(mx(hypot(a[0] - b[0], a[1] - b[1]) / 0.5, so2_dist64(a[2], b[2]) / 0.5), so2_dist64(a[3], b[3]) / 0.5);
+  } else if constexpr (KIND == DPG_ROBOT_QUAD2D) {
+    return mx(mx(hypot(a[0] - b[0], a[1] - b[1]) / 2.0, so2_dist64(a[2], b[2]) / 4.0),
+              mx(hypot(a[3] - b[3], a[4] - b[4]) / 4.0, fabs(a[5] - b[5]) / 8.0));
+  } else {
+    auto n3 = [](double x, double y, double z) {
+      return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+    };
+    double dq = fabs(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[3], b[3]), __dmul_rn(a[4], b[4])), __dmul_rn(a[5], b[5])),
+                               __dmul_rn(a[6], b[6])));
+    dq = dq < 1.0 ? dq : 1.0;
+    return mx(mx(n3(a[0] - b[0], a[1] - b[1], a[2] - b[2]) / 4.0, acos(dq) / 8.0),
+              mx(n3(a[7] - b[7], a[8] - b[8], a[9] - b[9]) / 4.0, n3(a[10] - b[10], a[11] - b[11], a[12] - b[12]) / 8.0));
   }
 }
-bool has_vel(int kind) { return kind == DPG_ROBOT_QUAD2D || kind == DPG_ROBOT_QUAD3D; }
 
-// state k of primitive p applied at node x (FP64, the transform of the tables)
-void transformed_state(const dpg_robot_desc &r, const std::vector<double> &st, int64_t row0, int k,
-                       const double *x, double *out) {
-  const int nx = r.nx;
-  std::memcpy(out, st.data() + (row0 + k) * nx, sizeof(double) * nx);
-  int pos[3], vel[3];
-  const int d = offset_comps(r.kind, pos, vel);
-  const bool v = has_vel(r.kind);
-  const double t = k * r.dt;
-  for (int i = 0; i < d; i++) {
-    out[pos[i]] += x[pos[i]];
-    if (v) {
-      out[pos[i]] += t * x[vel[i]];
-      out[vel[i]] += x[vel[i]];
-    }
+// the time lower bound in FP32 (the rewire filter's first test)
+template <int KIND>
+__device__ float lbt32(const float *a, const float *b) {
+  auto so2f = [](float x, float y) {
+    float d = fabsf(x - y);
+    if (d >= 6.2831853071795865f) d = fmodf(d, 6.2831853071795865f);
+    return d > 3.1415926535897932f ? 6.2831853071795865f - d : d;
+  };
+  if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
+    return fmaxf(hypotf(a[0] - b[0], a[1] - b[1]) * 2.f, so2f(a[2], b[2]) * 2.f);
+  } else if constexpr (KIND == DPG_ROBOT_CAR1) {
+    return fmaxf(fmaxf(hypotf(a[0] - b[0], a[1] - b[1]) * 2.f, so2f(a[2], b[2]) * 2.f), so2f(a[3], b[3]) * 2.f);
+  } else if constexpr (KIND == DPG_ROBOT_QUAD2D) {
+    return fmaxf(fmaxf(hypotf(a[0] - b[0], a[1] - b[1]) * 0.5f, so2f(a[2], b[2]) * 0.25f),
+                 fmaxf(hypotf(a[3] - b[3], a[4] - b[4]) * 0.25f, fabsf(a[5] - b[5]) * 0.125f));
+  } else {
+    auto l3 = [](float x, float y, float z) { return sqrtf(x * x + y * y + z * z); };
+    const float dq = fminf(1.f, fabsf(a[3] * b[3] + a[4] * b[4] + a[5] * b[5] + a[6] * b[6]));
+    return fmaxf(fmaxf(l3(a[0] - b[0], a[1] - b[1], a[2] - b[2]) * 0.25f, acosf(dq) * 0.125f),
+                 fmaxf(l3(a[7] - b[7], a[8] - b[8], a[9] - b[9]) * 0.25f,
+                       l3(a[10] - b[10], a[11] - b[11], a[12] - b[12]) * 0.125f));
   }
 }
 
@@ -167,7 +185,8 @@ static __global__ void grid_scatter(int n, const int *cell_of, const int *start,
 template <int KIND>
 __global__ void grid_query(RobotParams rp, float4 w32, Grid g, const double *q64, const float *q32, int Q,
                            const double *t64, const float *t32, const int *start, const int *cnt, const int *sorted,
-                           double radius, float band, int lower_only, const int64_t *offset, int *count, int *ids) {
+                           double radius, float band, int lower_only, const double *gq, const float *gsnap,
+                           const int64_t *offset, int *count, int *count_all, int *ids, double *lbt_out) {
   using R = Robot<KIND>;
   const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (q >= Q) return;
@@ -177,7 +196,8 @@ __global__ void grid_query(RobotParams rp, float4 w32, Grid g, const double *q64
   int c0[3] = {0, 0, 0};
 #pragma unroll
   for (int d = 0; d < R::POSD; d++) c0[d] = grid_coord<KIND>(g, a, d);
-  int n_in = 0;
+  int n_in = 0, n_keep = 0;
+  const float gq32 = gq ? (float)gq[q] : 0.f;
   const int zr = R::POSD == 3 ? 1 : 0;
   for (int dz = -zr; dz <= zr; dz++)
     for (int dy = -1; dy <= 1; dy++)
@@ -202,12 +222,45 @@ __global__ void grid_query(RobotParams rp, float4 w32, Grid g, const double *q64
                 in = full_dist64<KIND>(rp, q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX) <= radius;
             }
           }
-          const unsigned m = __ballot_sync(0xffffffffu, in);
-          if (in && offset) ids[offset[q] + n_in + __popc(m & ((1u << lane) - 1u))] = t;
+          // rewire filter: a neighbour with g + lbt >= its g when the table
+          // was made (g only decreases) can never be rewired by this candidate
+          // (FP32 first: a neighbour clearly out by more than 1e-3 (1 + g)
+          // is dropped; the rest are decided, and their bound kept, in FP64)
+          bool keep = in;
+          double lb = 0.0;
+          if (in) {
+            bool exact = lbt_out != nullptr && offset != nullptr;  // unfiltered: bounds in the write pass only
+            if (gsnap) {
+              float b32[R::NX];
+#pragma unroll
+              for (int k = 0; k < R::NX; k++) b32[k] = t32[(int64_t)t * R::NX + k];
+              const float gs = gsnap[t];
+              if (gq32 + lbt32<KIND>(a, b32) > gs + 1e-3f * (1.f + fabsf(gs))) {
+                keep = false;
+                exact = false;
+              } else {
+                exact = true;
+              }
+            }
+            if (exact) {
+              lb = lbt_exact<KIND>(q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX);
+              if (gsnap) keep = __dadd_rn(gq[q], lb) < (double)gsnap[t];
+            }
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, in), mk = __ballot_sync(0xffffffffu, keep);
+          if (keep && offset) {
+            const int64_t at = offset[q] + n_keep + __popc(mk & ((1u << lane) - 1u));
+            ids[at] = t;
+            if (lbt_out) lbt_out[at] = lb;
+          }
           n_in += __popc(m);
+          n_keep += __popc(mk);
         }
       }
-  if (lane == 0 && !offset) count[q] = n_in;
+  if (lane == 0 && !offset) {
+    count[q] = n_keep;
+    if (count_all) count_all[q] = n_in;
+  }
 }
 
 template <class F> void with_kind_s(int kind, F &&f) {
@@ -232,12 +285,113 @@ struct HeapItem {
   float f, g;
   int id, version;
 };
+struct NbrLbt {  // a rewire candidate and the time lower bound to it
+  int id;
+  double lbt;
+};
 struct HeapCmp {  // lowest f first, then highest g (compareAStarNode)
   bool operator()(const HeapItem &a, const HeapItem &b) const {
     if (a.f != b.f) return a.f > b.f;
     return a.g < b.g;
   }
 };
+
+// ---- successors of a round on the GPU ------------------------------------
+// The host restatement's arithmetic, every product and sum rounded on its
+// own (no contraction), as the host restatement computes them.
+template <int KIND>
+__device__ void transform_exact(const RobotParams &rp, const double *st64, int64_t s0, int k, const double *x,
+                                double *o) {
+  using R = Robot<KIND>;
+  const double *c = st64 + (s0 + k) * R::NX;
+#pragma unroll
+  for (int j = 0; j < R::NX; j++) o[j] = c[j];
+  const double t = __dmul_rn((double)k, rp.dt);
+#pragma unroll
+  for (int i = 0; i < R::POSD; i++) {
+    o[i] = __dadd_rn(o[i], x[i]);
+    if (R::VELOFF) {
+      o[i] = __dadd_rn(o[i], __dmul_rn(t, x[R::vel_comp(i)]));
+      o[R::vel_comp(i)] = __dadd_rn(o[R::vel_comp(i)], x[R::vel_comp(i)]);
+    }
+  }
+}
+
+// the host `distance` (weighted sum of block distances), terms rounded on their own
+template <int KIND>
+__device__ double distance_exact(const RobotParams &rp, const double *a, const double *b) {
+  const double *w = rp.w;
+  if constexpr (KIND == DPG_ROBOT_UNICYCLE1) {
+    return __dadd_rn(__dmul_rn(w[0], hypot(a[0] - b[0], a[1] - b[1])), __dmul_rn(w[1], so2_dist64(a[2], b[2])));
+  } else if constexpr (KIND == DPG_ROBOT_CAR1) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(w[0], hypot(a[0] - b[0], a[1] - b[1])), __dmul_rn(w[1], so2_dist64(a[2], b[2]))),
+                     __dmul_rn(w[2], so2_dist64(a[3], b[3])));
+  } else if constexpr (KIND == DPG_ROBOT_QUAD2D) {
+    double d = __dadd_rn(__dmul_rn(w[0], hypot(a[0] - b[0], a[1] - b[1])), __dmul_rn(w[1], so2_dist64(a[2], b[2])));
+    d = __dadd_rn(d, __dmul_rn(w[2], hypot(a[3] - b[3], a[4] - b[4])));
+    return __dadd_rn(d, __dmul_rn(w[3], fabs(a[5] - b[5])));
+  } else {
+    auto n3 = [](double x, double y, double z) {
+      return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+    };
+    double dq = fabs(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[3], b[3]), __dmul_rn(a[4], b[4])), __dmul_rn(a[5], b[5])),
+                               __dmul_rn(a[6], b[6])));
+    dq = fmin(dq, 1.0);
+    double d = __dadd_rn(__dmul_rn(w[0], n3(a[0] - b[0], a[1] - b[1], a[2] - b[2])), __dmul_rn(w[1], acos(dq)));
+    d = __dadd_rn(d, __dmul_rn(w[2], n3(a[7] - b[7], a[8] - b[8], a[9] - b[9])));
+    return __dadd_rn(d, __dmul_rn(w[3], n3(a[10] - b[10], a[11] - b[11], a[12] - b[12])));
+  }
+}
+
+// Candidate i = (batch node cn[i], motion cp[i]): the motion's last state at
+// the node, or the first of its states at floor((k + 1) / 5 L), k = 0..3,
+// within goal_tol of the goal (check_goal, dbastar.cpp:492-512); the chosen
+// index (-1: the last state), the duration up to it, the time lower bound from
+// the node to the motion's start and from the state to the goal, and the
+// candidate's g = (g of the node when popped + duration) + cost_delta_factor x
+// that lower bound.  out rows [nx + 4]: state, chosen, cost, lbt from the node,
+// lbt to the goal; gq[i] = g; q64 / q32 = the state.
+template <int KIND>
+__global__ void prepare_successors(RobotParams rp, const double *st64, const int64_t *soff, const int32_t *len,
+                                   const double *bx, const float *gpop, const int *cn, const int *cp, int Q,
+                                   const double *goal, double goal_tol, double cdf, double *out, double *gq,
+                                   double *q64, float *q32) {
+  using R = Robot<KIND>;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Q) return;
+  const int p = cp[i], L = len[p];
+  const int64_t s0 = soff[p];
+  const double *x = bx + (int64_t)cn[i] * R::NX;
+  double *row = out + (int64_t)i * (R::NX + 4);
+  double xe[R::NX], xi[R::NX], x0[R::NX];
+  transform_exact<KIND>(rp, st64, s0, L - 1, x, xe);
+  transform_exact<KIND>(rp, st64, s0, 0, x, x0);
+  int chosen = -1;
+  for (int k = 0; k < 4; k++) {
+    const int idx = (int)__fmul_rn(__fdiv_rn((float)(k + 1), 5.0f), (float)L);
+    if (idx >= L) continue;
+    transform_exact<KIND>(rp, st64, s0, idx, x, xi);
+    if (distance_exact<KIND>(rp, xi, goal) <= goal_tol) {
+#pragma unroll
+      for (int j = 0; j < R::NX; j++) xe[j] = xi[j];
+      chosen = idx;
+      break;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < R::NX; j++) {
+    row[j] = xe[j];
+    q64[(int64_t)i * R::NX + j] = xe[j];
+    q32[(int64_t)i * R::NX + j] = (float)xe[j];
+  }
+  const double cost = __dmul_rn((double)(chosen != -1 ? chosen : L - 1), rp.dt);
+  const double lbt_par = lbt_exact<KIND>(x, x0);
+  row[R::NX] = (double)chosen;
+  row[R::NX + 1] = cost;
+  row[R::NX + 2] = lbt_par;
+  row[R::NX + 3] = lbt_exact<KIND>(xe, goal);
+  gq[i] = __dadd_rn(__dadd_rn((double)gpop[cn[i]], cost), __dmul_rn(cdf, lbt_par));
+}
 
 template <class T> struct DVec {  // growable device array
   T *p = nullptr;
@@ -260,13 +414,6 @@ template <class T> struct DVec {  // growable device array
 
 }  // namespace
 
-int dpg_ctx_host_states(dpg_ctx *c, std::vector<double> &out) {
-  out.resize((size_t)c->S * c->robot.nx);
-  cudaSetDevice(c->device);
-  return cudaMemcpy(out.data(), c->st64.p, sizeof(double) * out.size(), cudaMemcpyDeviceToHost) == cudaSuccess
-             ? DPG_OK
-             : DPG_ERR_CUDA;
-}
 
 extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *start, const double *goal,
                           dpg_mlp *mlp, dpg_search_result *res, int32_t *path_motion, double *path_state,
@@ -284,9 +431,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   };
   const dpg_robot_desc &r = c->robot;
   const int nx = r.nx, P = c->P;
-  std::vector<double> st;
-  int rc = dpg_ctx_host_states(c, st);
-  if (rc) return rc;
+  int rc = DPG_OK;
   const double goal_tol = o->delta_factor_goal * o->delta;
   const double nov_radius = (1.0 - o->alpha) * o->delta;
   std::mt19937 rng((uint32_t)o->seed);
@@ -334,15 +479,20 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
     });
     return true;
   };
+  // the table's g values as uploaded with each node: never below a node's
+  // current g (g only decreases), so the rewire filter against them is exact
+  DVec<float> gsnap;
   size_t uploaded = 0;
   auto sync_table = [&]() -> bool {
     const size_t n = nodes.size();
-    if (!t64.reserve(n * nx) || !t32.reserve(n * nx)) return false;
+    if (!t64.reserve(n * nx) || !t32.reserve(n * nx) || !gsnap.reserve(n)) return false;
     if (n > uploaded) {
-      std::vector<float> f(xs.begin() + uploaded * nx, xs.end());
+      std::vector<float> f(xs.begin() + uploaded * nx, xs.end()), gs(n - uploaded);
+      for (size_t i = uploaded; i < n; i++) gs[i - uploaded] = nodes[i].g;
       cudaMemcpy(t64.p + uploaded * nx, xs.data() + uploaded * nx, sizeof(double) * (n - uploaded) * nx,
                  cudaMemcpyHostToDevice);
       cudaMemcpy(t32.p + uploaded * nx, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice);
+      cudaMemcpy(gsnap.p + uploaded, gs.data(), sizeof(float) * gs.size(), cudaMemcpyHostToDevice);
       uploaded = n;
       return sort_by_cell(t32.p, (int)n, tab_cnt, tab_start, tab_fill, tab_cell, tab_sorted);
     }
@@ -367,7 +517,13 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   open.push({nodes[s0].f, nodes[s0].g, s0, 0});
 
   // per-iteration device buffers
-  DVec<double> q64, b64;
+  DVec<double> q64, b64, prep, goal_d, gq, lbt_tab, lbt_self;
+  DVec<float> gpop_d;
+  DVec<int> cand, cnt_all;
+  std::vector<int> cnp;
+  std::vector<double> prep_h;
+  if (!goal_d.reserve(nx)) return DPG_ERR_OOM;
+  cudaMemcpy(goal_d.p, goal, sizeof(double) * nx, cudaMemcpyHostToDevice);
   DVec<float> q32;
   DVec<int> cnt_tab, ids_tab, cnt_self, ids_self;
   DVec<int64_t> off_tab, off_self;
@@ -441,10 +597,17 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       std::sort(per_node[b].begin(), per_node[b].end());
       if (o->shuffle) std::shuffle(per_node[b].begin(), per_node[b].end(), rng);
     }
+    // the batch's states and g when popped on the device (successor
+    // preparation, features); a successor's g counts from its node's g at
+    // pop time
+    std::vector<float> gpop(B);
+    for (int b = 0; b < B; b++) gpop[b] = nodes[batch[b]].g;
+    if (!b64.reserve((size_t)B * nx) || !gpop_d.reserve(B)) return DPG_ERR_OOM;
+    cudaMemcpy(b64.p, bx.data(), sizeof(double) * bx.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(gpop_d.p, gpop.data(), sizeof(float) * B, cudaMemcpyHostToDevice);
     if (o->heuristic == DPG_HEU_MLP) {  // node features of the batch, goal-conditioned
       const double tm0 = elapsed_ms();
-      if (!b64.reserve((size_t)B * nx) || !feat.reserve((size_t)B * kMlpNodeFeat)) return DPG_ERR_OOM;
-      cudaMemcpy(b64.p, bx.data(), sizeof(double) * bx.size(), cudaMemcpyHostToDevice);
+      if (!feat.reserve((size_t)B * kMlpNodeFeat)) return DPG_ERR_OOM;
       if ((rc = dpg_mlp_node_features(c, b64.p, B, goal, feat.p))) return rc;
       res->mlp_ms += elapsed_ms() - tm0;
     }
@@ -458,76 +621,92 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
     std::vector<int> n_new(B, 0);
     std::vector<char> finished(B, 0);
     for (int b = 0; b < B; b++) finished[b] = per_node[b].empty();
-    std::vector<int> first(B + 1, 0), c_node, c_prim, c_chosen, nbr;
-    std::vector<double> c_x, c_x0, c_cost;
+    std::vector<int> first(B + 1, 0), c_node, c_prim, c_chosen;
+    std::vector<NbrLbt> nbl;
+    std::vector<double> c_x, c_cost, c_lbtpar, c_hlbt;
     while (std::find(finished.begin(), finished.end(), 0) != finished.end()) {
       // successors of the round: end state (or the state meeting the goal),
       // transformed motion start, cost
-      c_node.clear(); c_prim.clear(); c_chosen.clear(); c_x.clear(); c_x0.clear(); c_cost.clear();
+      const double tp0 = elapsed_ms();
+      c_node.clear(); c_prim.clear();
       for (int b = 0; b < B; b++) {
         first[b] = (int)c_prim.size();
         if (finished[b]) continue;
-        const double *x = &bx[(size_t)b * nx];
         const size_t e = std::min(per_node[b].size(), pos[b] + chunk[b]);
         for (size_t j = pos[b]; j < e; j++) {
-          const int p = per_node[b][j];
-          const int L = c->h_len[p];
-          const size_t q = c_prim.size();
           c_node.push_back(b);
-          c_prim.push_back(p);
-          c_x.resize((q + 1) * nx);
-          c_x0.resize((q + 1) * nx);
-          transformed_state(r, st, c->h_soff[p], L - 1, x, &c_x[q * nx]);
-          transformed_state(r, st, c->h_soff[p], 0, x, &c_x0[q * nx]);
-          // check_goal: states at floor((k+1)/(n+1) * L), k = 0..3 (dbastar.cpp:492-512)
-          int chosen = -1;
-          double xi[16];
-          for (int k = 0; k < 4; k++) {
-            const int idx = (int)((float)(k + 1) / 5.0f * (float)L);
-            if (idx >= L) continue;
-            transformed_state(r, st, c->h_soff[p], idx, x, xi);
-            if (distance(r, xi, goal) <= goal_tol) {
-              std::memcpy(&c_x[q * nx], xi, sizeof(double) * nx);
-              chosen = idx;
-              break;
-            }
-          }
-          c_chosen.push_back(chosen);
-          c_cost.push_back((chosen != -1 ? chosen : L - 1) * r.dt);
+          c_prim.push_back(per_node[b][j]);
         }
       }
       first[B] = (int)c_prim.size();
       const int Q = (int)c_prim.size();
-      if (Q == 0) break;
+      if (Q == 0) {
+        res->prepare_ms += elapsed_ms() - tp0;
+        break;
+      }
+      // on the GPU: every candidate's end (or goal) state, start state,
+      // goal-check index and cost; the states stay there as the query rows
+      const size_t prow = (size_t)nx + 4;
+      if (!q64.reserve((size_t)Q * nx) || !q32.reserve((size_t)Q * nx) || !cand.reserve(2 * (size_t)Q) ||
+          !prep.reserve((size_t)Q * prow) || !gq.reserve(Q))
+        return DPG_ERR_OOM;
+      cnp.resize(2 * (size_t)Q);
+      std::copy(c_node.begin(), c_node.end(), cnp.begin());
+      std::copy(c_prim.begin(), c_prim.end(), cnp.begin() + Q);
+      cudaMemcpy(cand.p, cnp.data(), sizeof(int) * cnp.size(), cudaMemcpyHostToDevice);
+      with_kind_s(r.kind, [&](auto Kd) {
+        constexpr int KIND = decltype(Kd)::value;
+        prepare_successors<KIND><<<(Q + 127) / 128, 128>>>(
+            c->rp, static_cast<const double *>(c->st64.p), static_cast<const int64_t *>(c->soff.p),
+            static_cast<const int32_t *>(c->len.p), b64.p, gpop_d.p, cand.p, cand.p + Q, Q, goal_d.p, goal_tol,
+            o->cost_delta_factor, prep.p, gq.p, q64.p, q32.p);
+      });
+      prep_h.resize((size_t)Q * prow);
+      if (cudaMemcpy(prep_h.data(), prep.p, sizeof(double) * prep_h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return DPG_ERR_CUDA;
+      c_x.resize((size_t)Q * nx);
+      c_chosen.resize(Q);
+      c_cost.resize(Q);
+      c_lbtpar.resize(Q);
+      c_hlbt.resize(Q);
+      for (int q = 0; q < Q; q++) {
+        const double *row = &prep_h[(size_t)q * prow];
+        std::memcpy(&c_x[(size_t)q * nx], row, sizeof(double) * nx);
+        c_chosen[q] = (int)row[nx];
+        c_cost[q] = row[nx + 1];
+        c_lbtpar[q] = row[nx + 2];
+        c_hlbt[q] = row[nx + 3];
+      }
+      res->prepare_ms += elapsed_ms() - tp0;
 
       // novelty: successors vs explored nodes, and vs earlier successors of
       // the round; the id capacity grows until every list is complete
       const double tn0 = elapsed_ms();
-      if (!sync_table() || !q64.reserve((size_t)Q * nx) || !q32.reserve((size_t)Q * nx) || !cnt_tab.reserve(Q) ||
-          !cnt_self.reserve(Q))
-        return DPG_ERR_OOM;
-      std::vector<float> qf(c_x.begin(), c_x.end());
-      cudaMemcpy(q64.p, c_x.data(), sizeof(double) * c_x.size(), cudaMemcpyHostToDevice);
-      cudaMemcpy(q32.p, qf.data(), sizeof(float) * qf.size(), cudaMemcpyHostToDevice);
+      if (!sync_table() || !cnt_tab.reserve(Q) || !cnt_self.reserve(Q) || !cnt_all.reserve(Q)) return DPG_ERR_OOM;
       // the round's successors sorted by cell too, for the lower-index query
       if (!sort_by_cell(q32.p, Q, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted)) return DPG_ERR_OOM;
-      // count pass, offsets on the host, write pass into packed lists
-      std::vector<int> ct(Q), cs(Q), it, is;
+      // count pass, offsets on the host, write pass into packed lists: the
+      // explored neighbours that pass the rewire filter (all of them are
+      // counted for the novelty test) and every earlier successor of the
+      // round within the radius, each with its time lower bound
+      std::vector<int> ct(Q), ca(Q), cs(Q), it, is;
+      std::vector<double> lt, ls;
       std::vector<int64_t> ot(Q), os(Q);
       const unsigned qblocks = (unsigned)((Q + 7) / 8);  // 8 warps of 32 lanes, a warp per query
       auto query = [&](const int64_t *off_t, const int64_t *off_s) {
         with_kind_s(r.kind, [&](auto Kd) {
           constexpr int KIND = decltype(Kd)::value;
           grid_query<KIND><<<qblocks, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, t64.p, t32.p, tab_start.p,
-                                             tab_cnt.p, tab_sorted.p, nov_radius, 1e-5f, 0, off_t, cnt_tab.p,
-                                             ids_tab.p);
+                                             tab_cnt.p, tab_sorted.p, nov_radius, 1e-5f, 0, gq.p, gsnap.p, off_t,
+                                             cnt_tab.p, cnt_all.p, ids_tab.p, lbt_tab.p);
           grid_query<KIND><<<qblocks, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, q64.p, q32.p, rnd_start.p,
-                                             rnd_cnt.p, rnd_sorted.p, nov_radius, 1e-5f, 1, off_s, cnt_self.p,
-                                             ids_self.p);
+                                             rnd_cnt.p, rnd_sorted.p, nov_radius, 1e-5f, 1, nullptr, nullptr, off_s,
+                                             cnt_self.p, nullptr, ids_self.p, lbt_self.p);
         });
       };
       query(nullptr, nullptr);
       cudaMemcpy(ct.data(), cnt_tab.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
+      cudaMemcpy(ca.data(), cnt_all.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
       if (cudaMemcpy(cs.data(), cnt_self.p, sizeof(int) * Q, cudaMemcpyDeviceToHost) != cudaSuccess)
         return DPG_ERR_CUDA;
       int64_t nt = 0, ns = 0;
@@ -538,6 +717,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
         ns += cs[i];
       }
       if (!ids_tab.reserve((size_t)std::max<int64_t>(nt, 1)) || !ids_self.reserve((size_t)std::max<int64_t>(ns, 1)) ||
+          !lbt_tab.reserve((size_t)std::max<int64_t>(nt, 1)) || !lbt_self.reserve((size_t)std::max<int64_t>(ns, 1)) ||
           !off_tab.reserve(Q) || !off_self.reserve(Q))
         return DPG_ERR_OOM;
       cudaMemcpy(off_tab.p, ot.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice);
@@ -545,8 +725,16 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       query(off_tab.p, off_self.p);
       it.resize((size_t)nt);
       is.resize((size_t)ns);
-      if (nt) cudaMemcpy(it.data(), ids_tab.p, sizeof(int) * nt, cudaMemcpyDeviceToHost);
-      if (ns) cudaMemcpy(is.data(), ids_self.p, sizeof(int) * ns, cudaMemcpyDeviceToHost);
+      lt.resize((size_t)nt);
+      ls.resize((size_t)ns);
+      if (nt) {
+        cudaMemcpy(it.data(), ids_tab.p, sizeof(int) * nt, cudaMemcpyDeviceToHost);
+        cudaMemcpy(lt.data(), lbt_tab.p, sizeof(double) * nt, cudaMemcpyDeviceToHost);
+      }
+      if (ns) {
+        cudaMemcpy(is.data(), ids_self.p, sizeof(int) * ns, cudaMemcpyDeviceToHost);
+        cudaMemcpy(ls.data(), lbt_self.p, sizeof(double) * ns, cudaMemcpyDeviceToHost);
+      }
       if (cudaGetLastError() != cudaSuccess) return DPG_ERR_CUDA;
       res->novelty_ms += elapsed_ms() - tn0;
 
@@ -571,6 +759,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       }
 
       // insert or rewire, in pop order and the motions' order (dbastar.cpp:809-919)
+      const double ti0 = elapsed_ms();
       std::vector<int> accepted_as(Q, -1);  // node id of an accepted successor
       for (int b = 0; b < B; b++) {
         if (finished[b]) continue;
@@ -578,18 +767,24 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
         for (int ci = first[b]; ci < first[b + 1]; ci++) {
           pos[b]++;
           const double *cx = &c_x[(size_t)ci * nx];
-          double h = (o->heuristic == DPG_HEU_BLIND) ? 0.0 : lower_bound_time(r, cx, goal);
+          double h = (o->heuristic == DPG_HEU_BLIND) ? 0.0 : c_hlbt[ci];
           if (o->heuristic == DPG_HEU_ROADMAP) h = hroad[ci];
           if (o->heuristic == DPG_HEU_MLP) h = std::max(h, kCtgScale * std::max(0.0, (double)pred[2 * (size_t)ci + 1]));
-          const double g = (double)nodes[parent].g + c_cost[ci] +
-                           o->cost_delta_factor * lower_bound_time(r, &xs[(size_t)parent * nx], &c_x0[(size_t)ci * nx]);
-          nbr.assign(it.begin() + ot[ci], it.begin() + ot[ci] + ct[ci]);
+          const double g = (double)gpop[b] + c_cost[ci] + o->cost_delta_factor * c_lbtpar[ci];
+          // rewire candidates: the filtered explored neighbours and the
+          // accepted earlier successors, by node id, with their lower bounds
+          nbl.clear();
+          for (int k = 0; k < ct[ci]; k++) nbl.push_back({it[ot[ci] + k], lt[ot[ci] + k]});
+          bool self_nbr = false;
           for (int k = 0; k < cs[ci]; k++) {
             const int other = is[os[ci] + k];
-            if (accepted_as[other] >= 0) nbr.push_back(accepted_as[other]);
+            if (accepted_as[other] >= 0) {
+              nbl.push_back({accepted_as[other], ls[os[ci] + k]});
+              self_nbr = true;
+            }
           }
-          std::sort(nbr.begin(), nbr.end());
-          if (nbr.empty() || c_chosen[ci] != -1) {
+          std::sort(nbl.begin(), nbl.end(), [](const NbrLbt &x, const NbrLbt &y) { return x.id < y.id; });
+          if ((ca[ci] == 0 && !self_nbr) || c_chosen[ci] != -1) {
             const int id = add_node(cx);
             Node &n = nodes[id];
             n.g = (float)g;
@@ -603,9 +798,9 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
             accepted_as[ci] = id;
             n_new[b]++;
           } else {
-            for (int nb : nbr) {
-              Node &n = nodes[nb];
-              const double tentative = g + lower_bound_time(r, cx, &xs[(size_t)nb * nx]);
+            for (const NbrLbt &e : nbl) {
+              Node &n = nodes[e.id];
+              const double tentative = g + e.lbt;
               if (tentative < n.g) {
                 n.g = (float)tentative;
                 n.f = n.g + n.h;
@@ -614,7 +809,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
                 n.inter = -1;
                 n.version++;
                 n.in_open = true;
-                open.push({n.f, n.g, nb, n.version});
+                open.push({n.f, n.g, e.id, n.version});
               }
             }
           }
@@ -623,6 +818,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
         if (n_new[b] >= limit || pos[b] >= per_node[b].size()) finished[b] = 1;
         else chunk[b] *= 2;  // chunk used up below the limit: a larger one next round
       }
+      res->insert_ms += elapsed_ms() - ti0;
     }
   }
   res->status = status;

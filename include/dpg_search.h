@@ -19,8 +19,14 @@
  * of a round run on the GPU through a uniform grid over position (cell side
  * radius / position weight, nodes counting-sorted by cell, a warp per query
  * over the neighbouring cells; FP32 with an FP64 re-test near the radius);
- * neighbour lists are complete: counted, then packed.  Insertion and
- * rewiring run on the host in that order.
+ * neighbour lists are complete: counted (the novelty test), then packed with
+ * the time lower bound to each neighbour.  A successor's g counts from its
+ * node's g when the batch was popped (with batch = 1 that is the node's g:
+ * no successor can lower it), so the GPU also drops the explored neighbours
+ * it could never rewire (g + lower bound >= their g when they entered the
+ * table; g only decreases).  Successor states, goal checks and lower bounds
+ * are computed on the GPU with the host arithmetic (no contraction);
+ * insertion and rewiring run on the host in order.
  * batch = 1 visits nodes and motions in the reference's order.
  */
 #ifndef DPG_SEARCH_H
@@ -79,6 +85,8 @@ typedef struct dpg_search_result {
   int64_t nodes;                  /* explored nodes created */
   int64_t checked_pairs;          /* (node, motion) pairs exact-checked */
   double time_ms, expand_ms, novelty_ms, mlp_ms;
+  double prepare_ms;              /* successor states, goal checks (host) */
+  double insert_ms;               /* insert / rewire and the open list (host) */
 } dpg_search_result;
 
 /* Plan from start to goal (nx doubles each) on the context's robot,

@@ -109,6 +109,7 @@ def search(m, prims, env, start, goal, delta, alpha=0.5, batch=1, limit=20, max_
             status = "SOLVED"
             break
         bx = np.array([X[i] for i in bat])
+        gpop = [float(g[i]) for i in bat]  # a successor's g counts from its node's g when popped
         res = ob.expand(m, prims, env, bx, alpha * delta)
         # candidates: valid pairs, node (pop) order, motions ascending
         cands = []
@@ -141,7 +142,7 @@ def search(m, prims, env, start, goal, delta, alpha=0.5, batch=1, limit=20, max_
                 for (cb, p, xe, x0, chosen, cost) in per[b][pos[b]:pos[b] + chunk[b]]:
                     pos[b] += 1
                     hh = f32(hfun(xe)) if hfun else (f32(lbt(m, xe, goal)) if heuristic == 0 else f32(0))
-                    gg = float(g[parent_i]) + cost + cdf * float(lbt(m, X[parent_i], x0))
+                    gg = gpop[b] + cost + cdf * float(lbt(m, X[parent_i], x0))
                     nbr = sorted(np.flatnonzero(distance(m, np.array(X), xe[None, :]) <= nov))
                     if not nbr or chosen != -1:
                         X.append(xe)
