@@ -684,7 +684,9 @@ def run_search(args, rank, world, local_rank):
                 "expands": int(sum(r["expands"] for r in rs)), "checked_pairs": int(sum(r["checked_pairs"] for r in rs)),
                 "expand_ms": sum(r["expand_ms"] for r in rs), "novelty_ms": sum(r["novelty_ms"] for r in rs),
                 "mlp_ms": sum(r["mlp_ms"] for r in rs), "prepare_ms": sum(r["prepare_ms"] for r in rs),
-                "insert_ms": sum(r["insert_ms"] for r in rs), "total_ms": sum(r["time_ms"] for r in rs)}
+                "insert_ms": sum(r["insert_ms"] for r in rs), "rounds": sum(r["rounds"] for r in rs),
+                "table_ms": sum(r["table_ms"] for r in rs), "query_ms": sum(r["query_ms"] for r in rs),
+                "total_ms": sum(r["time_ms"] for r in rs)}
     both = [i for i in range(len(eval_probs)) if rows["plain"][i]["solved"] and rows["mlp"][i]["solved"]]
     ratio = [rows["plain"][i]["time_ms"] / max(rows["mlp"][i]["time_ms"], 1e-3) for i in both]
     cost_ratio = [rows["mlp"][i]["cost"] / max(rows["plain"][i]["cost"], 1e-9) for i in both]

@@ -179,87 +179,105 @@ static __global__ void grid_scatter(int n, const int *cell_of, const int *start,
   sorted[start[c] + atomicAdd(&fill[c], 1)] = i;
 }
 
-// warp per query over the neighbouring cells (lower_only: targets t < q).
-// Count pass (offset == nullptr): count[q] = neighbours; write pass: the
-// neighbour ids packed at ids[offset[q] ...].
+// rows[sorted[j]] -> out[j]: the targets' FP32 rows in cell order
+static __global__ void gather_rows(const float *rows, const int *sorted, int n, int nx, float *out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)n * nx) return;
+  const int64_t j = i / nx;
+  out[i] = rows[(int64_t)sorted[j] * nx + (i - j * nx)];
+}
+
+// Block of 256 threads per query over the neighbouring cells (the 3 (2-D) or
+// 9 (3-D) runs of cells contiguous in the cell order; targets' FP32 rows in
+// cell order, so the loads are coalesced); lower_only: targets t < q.
+// Count pass (offset == nullptr): count[q] = the kept neighbours (all of them
+// without a filter), count_all[q] = every neighbour within the radius.  Write
+// pass: the kept neighbours' ids (and time lower bounds) at offset[q] + a slot
+// from the per-query counter fill[q] (zero on entry): the order within a list
+// is arbitrary, the host sorts each list by id.  Rewire filter (gsnap set):
+// a neighbour with g + lbt >= the g it entered the table with is dropped
+// (g only decreases, so it could never be rewired).
 template <int KIND>
-__global__ void grid_query(RobotParams rp, float4 w32, Grid g, const double *q64, const float *q32, int Q,
-                           const double *t64, const float *t32, const int *start, const int *cnt, const int *sorted,
-                           double radius, float band, int lower_only, const double *gq, const float *gsnap,
-                           const int64_t *offset, int *count, int *count_all, int *ids, double *lbt_out) {
+__global__ void __launch_bounds__(256) grid_query(RobotParams rp, float4 w32, Grid g, const double *q64,
+                                                  const float *q32, int Q, const double *t64, const float *ts32,
+                                                  const int *start, const int *cnt, const int *sorted, double radius,
+                                                  float band, int lower_only, const double *gq, const float *gsnap,
+                                                  const int64_t *offset, int *count, int *count_all, int *fill,
+                                                  int *ids, double *lbt_out) {
   using R = Robot<KIND>;
-  const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (q >= Q) return;
+  __shared__ int s_in, s_keep;
+  const int q = blockIdx.x;
+  if (threadIdx.x == 0) { s_in = 0; s_keep = 0; }
+  __syncthreads();
   float a[R::NX];
 #pragma unroll
   for (int i = 0; i < R::NX; i++) a[i] = q32[(int64_t)q * R::NX + i];
   int c0[3] = {0, 0, 0};
 #pragma unroll
   for (int d = 0; d < R::POSD; d++) c0[d] = grid_coord<KIND>(g, a, d);
-  int n_in = 0, n_keep = 0;
   const float gq32 = gq ? (float)gq[q] : 0.f;
+  int my_in = 0, my_keep = 0;
   const int zr = R::POSD == 3 ? 1 : 0;
   for (int dz = -zr; dz <= zr; dz++)
-    for (int dy = -1; dy <= 1; dy++)
-      for (int dx = -1; dx <= 1; dx++) {
-        const int cx = c0[0] + dx, cy = c0[1] + dy, cz = c0[2] + dz;
-        if (cx < 0 || cy < 0 || cz < 0 || cx >= g.n[0] || cy >= g.n[1] || (R::POSD == 3 && cz >= g.n[2])) continue;
-        const int cell = cx + g.n[0] * (cy + g.n[1] * cz);
-        const int s = start[cell], e = s + cnt[cell];
-        for (int j = s; j < e; j += 32) {
-          const int i = j + lane;
-          bool in = false;
-          int t = 0;
-          if (i < e) {
-            t = sorted[i];
-            if (!(lower_only && t >= q)) {
-              float b[R::NX];
+    for (int dy = -1; dy <= 1; dy++) {
+      const int cy = c0[1] + dy, cz = c0[2] + dz;
+      if (cy < 0 || cz < 0 || cy >= g.n[1] || (R::POSD == 3 && cz >= g.n[2])) continue;
+      const int x0 = max(c0[0] - 1, 0), x1 = min(c0[0] + 1, g.n[0] - 1);
+      const int row = g.n[0] * (cy + g.n[1] * cz);
+      const int s = start[row + x0], e = start[row + x1] + cnt[row + x1];
+      for (int j = s + (int)threadIdx.x; j < e; j += blockDim.x) {
+        const int t = sorted[j];
+        if (lower_only && t >= q) continue;
+        const float *b = ts32 + (int64_t)j * R::NX;
+        float bb[R::NX];
 #pragma unroll
-              for (int k = 0; k < R::NX; k++) b[k] = t32[(int64_t)t * R::NX + k];
-              const float d = full_dist32<KIND>(w32, a, b);
-              in = d <= (float)radius;
-              if (fabsf(d - (float)radius) <= band)
-                in = full_dist64<KIND>(rp, q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX) <= radius;
-            }
+        for (int k = 0; k < R::NX; k++) bb[k] = b[k];
+        const float d = full_dist32<KIND>(w32, a, bb);
+        bool in = d <= (float)radius;
+        if (fabsf(d - (float)radius) <= band)
+          in = full_dist64<KIND>(rp, q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX) <= radius;
+        if (!in) continue;
+        // (FP32 first: a neighbour clearly out by more than 1e-3 (1 + g) is
+        // dropped; the rest are decided, and their bound kept, in FP64)
+        bool keep = true, exact = lbt_out != nullptr && offset != nullptr;
+        double lb = 0.0;
+        if (gsnap) {
+          const float gs = gsnap[t];
+          if (gq32 + lbt32<KIND>(a, bb) > gs + 1e-3f * (1.f + fabsf(gs))) {
+            keep = false;
+            exact = false;
+          } else {
+            exact = true;
           }
-          // rewire filter: a neighbour with g + lbt >= its g when the table
-          // was made (g only decreases) can never be rewired by this candidate
-          // (FP32 first: a neighbour clearly out by more than 1e-3 (1 + g)
-          // is dropped; the rest are decided, and their bound kept, in FP64)
-          bool keep = in;
-          double lb = 0.0;
-          if (in) {
-            bool exact = lbt_out != nullptr && offset != nullptr;  // unfiltered: bounds in the write pass only
-            if (gsnap) {
-              float b32[R::NX];
-#pragma unroll
-              for (int k = 0; k < R::NX; k++) b32[k] = t32[(int64_t)t * R::NX + k];
-              const float gs = gsnap[t];
-              if (gq32 + lbt32<KIND>(a, b32) > gs + 1e-3f * (1.f + fabsf(gs))) {
-                keep = false;
-                exact = false;
-              } else {
-                exact = true;
-              }
-            }
-            if (exact) {
-              lb = lbt_exact<KIND>(q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX);
-              if (gsnap) keep = __dadd_rn(gq[q], lb) < (double)gsnap[t];
-            }
-          }
-          const unsigned m = __ballot_sync(0xffffffffu, in), mk = __ballot_sync(0xffffffffu, keep);
-          if (keep && offset) {
-            const int64_t at = offset[q] + n_keep + __popc(mk & ((1u << lane) - 1u));
-            ids[at] = t;
-            if (lbt_out) lbt_out[at] = lb;
-          }
-          n_in += __popc(m);
-          n_keep += __popc(mk);
+        }
+        if (exact) {
+          lb = lbt_exact<KIND>(q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX);
+          if (gsnap) keep = __dadd_rn(gq[q], lb) < (double)gsnap[t];
+        }
+        my_in++;
+        if (!keep) continue;
+        my_keep++;
+        if (offset) {
+          const int64_t at = offset[q] + atomicAdd(&fill[q], 1);
+          ids[at] = t;
+          if (lbt_out) lbt_out[at] = lb;
         }
       }
-  if (lane == 0 && !offset) {
-    count[q] = n_keep;
-    if (count_all) count_all[q] = n_in;
+    }
+  if (!offset) {
+    for (int o = 16; o > 0; o >>= 1) {
+      my_in += __shfl_down_sync(0xffffffffu, my_in, o);
+      my_keep += __shfl_down_sync(0xffffffffu, my_keep, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(&s_in, my_in);
+      atomicAdd(&s_keep, my_keep);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      count[q] = s_keep;
+      if (count_all) count_all[q] = s_in;
+    }
   }
 }
 
@@ -463,12 +481,17 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   }
   // cell-sorted copies of the explored nodes (t_*) and of a round's successors (s_*)
   DVec<int> tab_cnt, tab_start, tab_fill, tab_cell, tab_sorted, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted;
+  DVec<int> fill_tab, fill_self;
+  DVec<float> tab_rows, rnd_rows;
   if (!tab_cnt.reserve(n_cells) || !tab_start.reserve(n_cells) || !tab_fill.reserve(n_cells) ||
       !rnd_cnt.reserve(n_cells) || !rnd_start.reserve(n_cells) || !rnd_fill.reserve(n_cells))
     return DPG_ERR_OOM;
+  // counting sort of n rows by cell; rows_out = the FP32 rows in that order
   auto sort_by_cell = [&](const float *rows, int n, DVec<int> &cnt, DVec<int> &start, DVec<int> &fill,
-                          DVec<int> &cell, DVec<int> &sorted) -> bool {
-    if (!cell.reserve(std::max(n, 1)) || !sorted.reserve(std::max(n, 1))) return false;
+                          DVec<int> &cell, DVec<int> &sorted, DVec<float> &rows_out) -> bool {
+    if (!cell.reserve(std::max(n, 1)) || !sorted.reserve(std::max(n, 1)) ||
+        !rows_out.reserve((size_t)std::max(n, 1) * nx))
+      return false;
     cudaMemset(cnt.p, 0, sizeof(int) * n_cells);
     cudaMemset(fill.p, 0, sizeof(int) * n_cells);
     with_kind_s(r.kind, [&](auto Kd) {
@@ -476,6 +499,8 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       if (n > 0) grid_count<KIND><<<(n + 255) / 256, 256>>>(grid, rows, n, cell.p, cnt.p);
       grid_scan<<<1, 1024>>>(n_cells, cnt.p, start.p);
       if (n > 0) grid_scatter<<<(n + 255) / 256, 256>>>(n, cell.p, start.p, fill.p, sorted.p);
+      if (n > 0)
+        gather_rows<<<(unsigned)(((int64_t)n * nx + 255) / 256), 256>>>(rows, sorted.p, n, nx, rows_out.p);
     });
     return true;
   };
@@ -494,7 +519,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       cudaMemcpy(t32.p + uploaded * nx, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice);
       cudaMemcpy(gsnap.p + uploaded, gs.data(), sizeof(float) * gs.size(), cudaMemcpyHostToDevice);
       uploaded = n;
-      return sort_by_cell(t32.p, (int)n, tab_cnt, tab_start, tab_fill, tab_cell, tab_sorted);
+      return sort_by_cell(t32.p, (int)n, tab_cnt, tab_start, tab_fill, tab_cell, tab_sorted, tab_rows);
     }
     return true;
   };
@@ -682,9 +707,14 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       // novelty: successors vs explored nodes, and vs earlier successors of
       // the round; the id capacity grows until every list is complete
       const double tn0 = elapsed_ms();
+      res->rounds++;
+      const double tt0 = elapsed_ms();
       if (!sync_table() || !cnt_tab.reserve(Q) || !cnt_self.reserve(Q) || !cnt_all.reserve(Q)) return DPG_ERR_OOM;
+      res->table_ms += elapsed_ms() - tt0;
       // the round's successors sorted by cell too, for the lower-index query
-      if (!sort_by_cell(q32.p, Q, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted)) return DPG_ERR_OOM;
+      if (!sort_by_cell(q32.p, Q, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted, rnd_rows) ||
+          !fill_tab.reserve(Q) || !fill_self.reserve(Q))
+        return DPG_ERR_OOM;
       // count pass, offsets on the host, write pass into packed lists: the
       // explored neighbours that pass the rewire filter (all of them are
       // counted for the novelty test) and every earlier successor of the
@@ -692,18 +722,22 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       std::vector<int> ct(Q), ca(Q), cs(Q), it, is;
       std::vector<double> lt, ls;
       std::vector<int64_t> ot(Q), os(Q);
-      const unsigned qblocks = (unsigned)((Q + 7) / 8);  // 8 warps of 32 lanes, a warp per query
-      auto query = [&](const int64_t *off_t, const int64_t *off_s) {
+      auto query = [&](const int64_t *off_t, const int64_t *off_s) {  // a block per query
+        if (off_t) {
+          cudaMemsetAsync(fill_tab.p, 0, sizeof(int) * Q);
+          cudaMemsetAsync(fill_self.p, 0, sizeof(int) * Q);
+        }
         with_kind_s(r.kind, [&](auto Kd) {
           constexpr int KIND = decltype(Kd)::value;
-          grid_query<KIND><<<qblocks, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, t64.p, t32.p, tab_start.p,
-                                             tab_cnt.p, tab_sorted.p, nov_radius, 1e-5f, 0, gq.p, gsnap.p, off_t,
-                                             cnt_tab.p, cnt_all.p, ids_tab.p, lbt_tab.p);
-          grid_query<KIND><<<qblocks, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, q64.p, q32.p, rnd_start.p,
-                                             rnd_cnt.p, rnd_sorted.p, nov_radius, 1e-5f, 1, nullptr, nullptr, off_s,
-                                             cnt_self.p, nullptr, ids_self.p, lbt_self.p);
+          grid_query<KIND><<<(unsigned)Q, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, t64.p, tab_rows.p, tab_start.p,
+                                                 tab_cnt.p, tab_sorted.p, nov_radius, 1e-5f, 0, gq.p, gsnap.p, off_t,
+                                                 cnt_tab.p, cnt_all.p, fill_tab.p, ids_tab.p, lbt_tab.p);
+          grid_query<KIND><<<(unsigned)Q, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, q64.p, rnd_rows.p, rnd_start.p,
+                                                 rnd_cnt.p, rnd_sorted.p, nov_radius, 1e-5f, 1, nullptr, nullptr,
+                                                 off_s, cnt_self.p, nullptr, fill_self.p, ids_self.p, lbt_self.p);
         });
       };
+      const double tq0 = elapsed_ms();
       query(nullptr, nullptr);
       cudaMemcpy(ct.data(), cnt_tab.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
       cudaMemcpy(ca.data(), cnt_all.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
@@ -736,6 +770,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
         cudaMemcpy(ls.data(), lbt_self.p, sizeof(double) * ns, cudaMemcpyDeviceToHost);
       }
       if (cudaGetLastError() != cudaSuccess) return DPG_ERR_CUDA;
+      res->query_ms += elapsed_ms() - tq0;
       res->novelty_ms += elapsed_ms() - tn0;
 
       // learned heuristic: the surrogate's cost-to-go of every (node, motion)

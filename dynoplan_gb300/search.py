@@ -25,7 +25,8 @@ class SearchResult(C.Structure):
                 ("path_len", C.c_int32), ("expands", C.c_int64), ("nodes", C.c_int64),
                 ("checked_pairs", C.c_int64), ("time_ms", C.c_double), ("expand_ms", C.c_double),
                 ("novelty_ms", C.c_double), ("mlp_ms", C.c_double), ("prepare_ms", C.c_double),
-                ("insert_ms", C.c_double)]
+                ("insert_ms", C.c_double), ("rounds", C.c_int64), ("table_ms", C.c_double),
+                ("query_ms", C.c_double)]
 
 
 def options(delta, alpha=0.5, batch=1, heuristic=HEU_EUCLIDEAN, limit_branching_factor=20,

@@ -87,6 +87,9 @@ typedef struct dpg_search_result {
   double time_ms, expand_ms, novelty_ms, mlp_ms;
   double prepare_ms;              /* successor states, goal checks (host) */
   double insert_ms;               /* insert / rewire and the open list (host) */
+  int64_t rounds;                 /* successor rounds (one novelty query each) */
+  double table_ms;                /* novelty: explored-node table upload and cell sort */
+  double query_ms;                /* novelty: the two query passes and their copies */
 } dpg_search_result;
 
 /* Plan from start to goal (nx doubles each) on the context's robot,
