@@ -123,9 +123,10 @@ __device__ float lbt32(const float *a, const float *b) {
 // Every metric here is >= w0 * |position difference|, so a target within
 // `radius` lies in the query's cell or a neighbouring one when the cell side
 // is radius / w0 (slightly enlarged for rounding).  Each round the targets
-// are counting-sorted by cell (count, scan, scatter); a warp per query scans
-// the 3^POSD neighbouring cells' contiguous ranges.  Neighbour lists are
-// sorted on the host, so the order within a cell does not matter.
+// are counting-sorted by cell (count, scan, scatter, rows gathered into that
+// order); a block per query scans the neighbouring cells' contiguous ranges.
+// Neighbour lists are sorted on the host, so the order within a list does
+// not matter.
 struct Grid {
   float lo[3];
   float inv_cs;

@@ -17,8 +17,9 @@
  * in pop order, visits its next chunk of valid motions (2 x the limit,
  * doubling per round) until it has `limit` new nodes.  The novelty queries
  * of a round run on the GPU through a uniform grid over position (cell side
- * radius / position weight, nodes counting-sorted by cell, a warp per query
- * over the neighbouring cells; FP32 with an FP64 re-test near the radius);
+ * radius / position weight, nodes counting-sorted by cell, a block of
+ * threads per query over the neighbouring cells; FP32 with an FP64 re-test
+ * near the radius);
  * neighbour lists are complete: counted (the novelty test), then packed with
  * the time lower bound to each neighbour.  A successor's g counts from its
  * node's g when the batch was popped (with batch = 1 that is the node's g:
