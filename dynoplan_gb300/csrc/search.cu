@@ -198,13 +198,16 @@ static __global__ void gather_rows(const float *rows, const int *sorted, int n, 
 // is arbitrary, the host sorts each list by id.  Rewire filter (gsnap set):
 // a neighbour with g + lbt >= the g it entered the table with is dropped
 // (g only decreases, so it could never be rewired).
+// t_ok (lower_only queries): targets that can still be accepted as new nodes
+// this round; the others are skipped (a successor with an explored neighbour
+// in the radius and no goal hit is never accepted).
 template <int KIND>
 __global__ void __launch_bounds__(256) grid_query(RobotParams rp, float4 w32, Grid g, const double *q64,
                                                   const float *q32, int Q, const double *t64, const float *ts32,
                                                   const int *start, const int *cnt, const int *sorted, double radius,
-                                                  float band, int lower_only, const double *gq, const float *gsnap,
-                                                  const int64_t *offset, int *count, int *count_all, int *fill,
-                                                  int *ids, double *lbt_out) {
+                                                  float band, int lower_only, const unsigned char *t_ok,
+                                                  const double *gq, const float *gsnap, const int64_t *offset,
+                                                  int *count, int *count_all, int *fill, int *ids, double *lbt_out) {
   using R = Robot<KIND>;
   __shared__ int s_in, s_keep;
   const int q = blockIdx.x;
@@ -228,7 +231,7 @@ __global__ void __launch_bounds__(256) grid_query(RobotParams rp, float4 w32, Gr
       const int s = start[row + x0], e = start[row + x1] + cnt[row + x1];
       for (int j = s + (int)threadIdx.x; j < e; j += blockDim.x) {
         const int t = sorted[j];
-        if (lower_only && t >= q) continue;
+        if (lower_only && (t >= q || (t_ok && !t_ok[t]))) continue;
         const float *b = ts32 + (int64_t)j * R::NX;
         float bb[R::NX];
 #pragma unroll
@@ -280,6 +283,15 @@ __global__ void __launch_bounds__(256) grid_query(RobotParams rp, float4 w32, Gr
       if (count_all) count_all[q] = s_in;
     }
   }
+}
+
+// ok[i] = successor i can be accepted as a new node: no explored neighbour in
+// the radius, or it meets the goal (chosen index != -1, prep rows of width prow)
+static __global__ void acceptable(int Q, const int *count_all, const double *prep, int prow, int nx,
+                                  unsigned char *ok) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Q) return;
+  ok[i] = (count_all[i] == 0 || prep[(int64_t)i * prow + nx] != -1.0) ? 1 : 0;
 }
 
 template <class F> void with_kind_s(int kind, F &&f) {
@@ -483,6 +495,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   // cell-sorted copies of the explored nodes (t_*) and of a round's successors (s_*)
   DVec<int> tab_cnt, tab_start, tab_fill, tab_cell, tab_sorted, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted;
   DVec<int> fill_tab, fill_self;
+  DVec<unsigned char> ok_d;
   DVec<float> tab_rows, rnd_rows;
   if (!tab_cnt.reserve(n_cells) || !tab_start.reserve(n_cells) || !tab_fill.reserve(n_cells) ||
       !rnd_cnt.reserve(n_cells) || !rnd_start.reserve(n_cells) || !rnd_fill.reserve(n_cells))
@@ -714,7 +727,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       res->table_ms += elapsed_ms() - tt0;
       // the round's successors sorted by cell too, for the lower-index query
       if (!sort_by_cell(q32.p, Q, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted, rnd_rows) ||
-          !fill_tab.reserve(Q) || !fill_self.reserve(Q))
+          !fill_tab.reserve(Q) || !fill_self.reserve(Q) || !ok_d.reserve(Q))
         return DPG_ERR_OOM;
       // count pass, offsets on the host, write pass into packed lists: the
       // explored neighbours that pass the rewire filter (all of them are
@@ -731,11 +744,15 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
         with_kind_s(r.kind, [&](auto Kd) {
           constexpr int KIND = decltype(Kd)::value;
           grid_query<KIND><<<(unsigned)Q, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, t64.p, tab_rows.p, tab_start.p,
-                                                 tab_cnt.p, tab_sorted.p, nov_radius, 1e-5f, 0, gq.p, gsnap.p, off_t,
-                                                 cnt_tab.p, cnt_all.p, fill_tab.p, ids_tab.p, lbt_tab.p);
+                                                 tab_cnt.p, tab_sorted.p, nov_radius, 1e-5f, 0, nullptr, gq.p,
+                                                 gsnap.p, off_t, cnt_tab.p, cnt_all.p, fill_tab.p, ids_tab.p,
+                                                 lbt_tab.p);
+          // which successors can be accepted follows from the explored-table counts
+          if (!off_t) acceptable<<<(Q + 255) / 256, 256>>>(Q, cnt_all.p, prep.p, (int)prow, nx, ok_d.p);
           grid_query<KIND><<<(unsigned)Q, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, q64.p, rnd_rows.p, rnd_start.p,
-                                                 rnd_cnt.p, rnd_sorted.p, nov_radius, 1e-5f, 1, nullptr, nullptr,
-                                                 off_s, cnt_self.p, nullptr, fill_self.p, ids_self.p, lbt_self.p);
+                                                 rnd_cnt.p, rnd_sorted.p, nov_radius, 1e-5f, 1, ok_d.p, nullptr,
+                                                 nullptr, off_s, cnt_self.p, nullptr, fill_self.p, ids_self.p,
+                                                 lbt_self.p);
         });
       };
       const double tq0 = elapsed_ms();
