@@ -25,7 +25,9 @@
  * node's g when the batch was popped (with batch = 1 that is the node's g:
  * no successor can lower it), so the GPU also drops the explored neighbours
  * it could never rewire (g + lower bound >= their g when they entered the
- * table; g only decreases).  Successor states, goal checks and lower bounds
+ * table; g only decreases), and lists a round's earlier successors only where
+ * they can still be accepted (no explored neighbour, or a goal hit).
+ * Successor states, goal checks and lower bounds
  * are computed on the GPU with the host arithmetic (no contraction);
  * insertion and rewiring run on the host in order.
  * batch = 1 visits nodes and motions in the reference's order.
