@@ -69,9 +69,12 @@ def canonical_table(m, prims):
 
 
 def search(m, prims, env, start, goal, delta, alpha=0.5, batch=1, limit=20, max_expands=100000,
-           heuristic=0, dfg=1.0, cdf=1.0, hfun=None):
+           heuristic=0, dfg=1.0, cdf=1.0, hfun=None, g_at_pop=True):
     """heuristic 0: time lower bound to the goal, -1: blind; hfun(x), when
-    given, replaces both (the roadmap heuristic's restatement)"""
+    given, replaces both (the roadmap heuristic's restatement).  g_at_pop:
+    a successor's g counts from its node's g when the batch was popped (the
+    GPU search's rule); False reads the node's current g, as the reference's
+    one-node loop does -- the same thing when batch = 1."""
     table = canonical_table(m, prims)
     f32 = np.float32
     X = [np.asarray(start, float)]
@@ -142,7 +145,8 @@ def search(m, prims, env, start, goal, delta, alpha=0.5, batch=1, limit=20, max_
                 for (cb, p, xe, x0, chosen, cost) in per[b][pos[b]:pos[b] + chunk[b]]:
                     pos[b] += 1
                     hh = f32(hfun(xe)) if hfun else (f32(lbt(m, xe, goal)) if heuristic == 0 else f32(0))
-                    gg = gpop[b] + cost + cdf * float(lbt(m, X[parent_i], x0))
+                    gp = gpop[b] if g_at_pop else float(g[parent_i])
+                    gg = gp + cost + cdf * float(lbt(m, X[parent_i], x0))
                     nbr = sorted(np.flatnonzero(distance(m, np.array(X), xe[None, :]) <= nov))
                     if not nbr or chosen != -1:
                         X.append(xe)
