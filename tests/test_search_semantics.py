@@ -17,7 +17,7 @@ def test_g_at_pop_equals_current_g_with_one_node_per_iteration(kind, seed):
     runs = [search_ref.search(m, prims, env, se[0], se[1], 0.5, batch=1, max_expands=300, g_at_pop=rule)
             for rule in (True, False)]
     a, b = runs
-    assert a["expands"] > 100  # a search that explores, rewires and (here) solves or runs out
+    assert a["expands"] > 100  # searches that explore well beyond the start
     for k in ("status", "expands", "nodes", "solved"):
         assert a[k] == b[k], k
     if a["solved"]:
