@@ -1,16 +1,20 @@
 // expand_kernels.cuh -- sm_103a kernels of the batched db-A* expansion.
 //
 // Pipeline for one dpg_expand (N frontier states x P primitives):
-//   prep_nodes      node keys / offsets, component-major FP32
-//   nn_mask         ball membership bitmask M[word][prim] + per-(node tile,
-//                   prim) counts; FP64 re-test of |d - r| <= ball_band
-//   nn_prefix       per-primitive exclusive prefix over node tiles
-//   scan_totals     per-primitive bases in length order, work-item bases
 //   (node_tiles, nn_prefix, cell_scan, cell_scatter, gather_nodes: batches
 //    of >= kReorderMin nodes are processed in spatial order)
+//   prep_nodes      node keys / offsets, component-major FP32
+//   nn_grid         ball membership through the primitives' key-space grid
+//                   (batches >= 2048 nodes, one- or two-component keys), or
+//   nn_mask         the same by testing every primitive: bitmask
+//                   M[prim][word] + per-(node tile, prim) counts; FP64 re-test
+//                   of |d - r| <= ball_band
+//   nn_prefix       per-primitive exclusive prefix over node tiles
+//   scan_totals     per-primitive bases in length order, work-item bases
 //   nn_emit         pair lists grouped by primitive, nodes in processing order
 //   check_pairs     persistent warps over (primitive, 32 nodes) work items
-//                   (check_kernels.cuh)
+//                   (check_kernels.cuh); they also restore the caller's node
+//                   ids of a spatially ordered batch
 //
 // The reference does this per node with a KD-tree radius query and a
 // per-motion fcl AABB tree (include/dynoplan/dbastar/dbastar.hpp:270-312,
