@@ -30,8 +30,11 @@
  *     are owned by the caller (host or device memory, see dpg_expand_opts).
  *   - Precision: DPG_FP32 computes rollouts and separating-axis tests in
  *     FP32 and recomputes in FP64, on the GPU, every pair whose gap or
- *     bounds margin lies within contact_band of zero and every ball test
- *     within ball_band of the radius; DPG_FP64 computes everything in FP64.
+ *     bounds margin lies within contact_band of zero; DPG_FP64 computes the
+ *     transforms, bounds and collision tests and the end states in FP64.
+ *     In both modes the ball test runs in FP32 and is decided in FP64 when
+ *     the distance lies within ball_band of the radius, so the neighbour
+ *     sets are those of an FP64 test.
  */
 #ifndef DPG_H
 #define DPG_H
