@@ -324,7 +324,7 @@ def run_ours(args, rank, world, local_rank):
     ctx.upload_primitives(wl.prims)
     ctx.upload_env(wl.env)
     prec = wl.precision
-    es_bytes = 8 if prec == 1 else 4
+    es_bytes = 8 if prec != 0 else 4
 
     # size the outputs from one probing call
     probe = ctx.expand(wl.nodes, wl.radius, precision=prec)
@@ -338,7 +338,7 @@ def run_ours(args, rank, world, local_rank):
         "prim": torch.empty(cap, dtype=torch.int32, device=dev),
         "verdict": torch.empty(cap, dtype=torch.uint8, device=dev),
         "first_invalid": torch.empty(cap, dtype=torch.int16, device=dev),
-        "end_state": torch.empty((cap, nx), dtype=torch.float64 if prec == 1 else torch.float32, device=dev),
+        "end_state": torch.empty((cap, nx), dtype=torch.float64 if prec != 0 else torch.float32, device=dev),
         "min_gap": torch.empty(cap, dtype=torch.float32, device=dev),
         "flags": torch.empty(cap, dtype=torch.uint8, device=dev),
     }
@@ -449,7 +449,7 @@ def run_radius_variant(args, lib, ctx, wl, x_d, prec, dev):
         "prim": torch.empty(cap, dtype=torch.int32, device=dev),
         "verdict": torch.empty(cap, dtype=torch.uint8, device=dev),
         "first_invalid": torch.empty(cap, dtype=torch.int16, device=dev),
-        "end_state": torch.empty((cap, nx), dtype=torch.float64 if prec == 1 else torch.float32, device=dev),
+        "end_state": torch.empty((cap, nx), dtype=torch.float64 if prec != 0 else torch.float32, device=dev),
         "min_gap": torch.empty(cap, dtype=torch.float32, device=dev),
         "flags": torch.empty(cap, dtype=torch.uint8, device=dev),
     }
@@ -475,7 +475,7 @@ def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
     hosts = {
         "node": G.PinnedArray(cap, np.uint32), "prim": G.PinnedArray(cap, np.uint32),
         "verdict": G.PinnedArray(cap, np.uint8), "first_invalid": G.PinnedArray(cap, np.int16),
-        "end_state": G.PinnedArray((cap, nx), np.float64 if prec == 1 else np.float32),
+        "end_state": G.PinnedArray((cap, nx), np.float64 if prec != 0 else np.float32),
         "min_gap": G.PinnedArray(cap, np.float32), "flags": G.PinnedArray(cap, np.uint8),
     }
     host_out = {k: v.array for k, v in hosts.items()}

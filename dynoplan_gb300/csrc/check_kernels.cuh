@@ -176,7 +176,9 @@ __device__ __forceinline__ bool near_box(const float *cen, const float *hf, cons
 
 // NW: words of the per-lane obstacle bitmasks (obstacles <= 32 NW); 0 = no
 // culling (more than kMaxCullObs obstacles), every state tests every obstacle.
-template <int KIND, class Real, bool BAND, int NW, bool LOCKSTEP>
+// ES64: write the end state in FP64 (the FP64 canonical row plus the FP64
+// node offset) while the tests run in Real.
+template <int KIND, class Real, bool BAND, int NW, bool LOCKSTEP, bool ES64 = false>
 __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t pair, uint32_t node,
                           bool active) {
   using R = Robot<KIND>;
@@ -411,7 +413,23 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
     o.min_gap[row_out] = verdict == DPG_OUT_OF_BOUNDS ? __int_as_float(0x7fc00000)
                                                    : ((float)mg <= kGapCap ? (float)mg : __int_as_float(0x7f800000));
   if (o.flags) o.flags[row_out] = rechecked ? DPG_FLAG_CONTACT_RECHECK : 0;
-  if (o.end_state) {
+  if (ES64 && o.end_state) {
+    double *es = (double *)o.end_state + row_out * R::NX;
+    const double t = double(er) * rp.dt;
+    const double *xs = pv.st64 + (s0 + er) * R::NX;
+#pragma unroll
+    for (int c = 0; c < R::NX; c++) {
+      double v = xs[c];
+      if (c < D) {
+        v += x64[c];
+        if (V) v += t * x64[R::vel_comp(c)];
+      }
+#pragma unroll
+      for (int i = 0; i < V; i++)
+        if (c == R::vel_comp(i)) v += x64[R::vel_comp(i)];
+      es[c] = v;
+    }
+  } else if (o.end_state) {
     Real *es = (Real *)o.end_state + row_out * R::NX;
     const Real t = Real(er) * dtR;
     const int64_t row = s0 + er;
@@ -446,7 +464,7 @@ __device__ void load_obstacles(const EnvView &ev, void *sm) {
 }
 
 // Persistent warps over (primitive, 32 nodes) work items.
-template <int KIND, class Real, bool BAND, int NW>
+template <int KIND, class Real, bool BAND, int NW, bool ES64 = false>
 __global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) check_pairs(CheckArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   load_obstacles<Real, KIND>(A.ev, smem);
@@ -482,7 +500,7 @@ __global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) chec
     const unsigned long long pair = first + lane;
     const bool active = pair < end;
     const uint32_t node = active ? A.out.node[pair] : 0u;
-    check_one<KIND, Real, BAND, NW, true>(A, smem, p, (int64_t)pair, node, active);
+    check_one<KIND, Real, BAND, NW, true, ES64>(A, smem, p, (int64_t)pair, node, active);
   }
 }
 

@@ -17,6 +17,7 @@
 #include "dpg_mlp.h"
 #include "mlp_kernels.cuh"
 
+#include "check_list.h"
 #include "ctx.h"
 
 using namespace dpg;
@@ -112,8 +113,12 @@ template <class F> void with_kind(int kind, F &&f) {
 // The exact check of the pair list on `st`: lockstep warps over (primitive,
 // 32 nodes) items, with obstacle culling when the candidate masks cover
 // every obstacle.
+// prec: DPG_FP32 (FP32 tests, FP64 decisions in the band, FP32 end states),
+// DPG_FP64 (the same tests, FP64 end states), DPG_FP64_STRICT (every test in
+// FP64).
 template <int KIND>
-static void launch_check(dpg_ctx *c, const CheckArgs &ca, bool fp64, cudaStream_t st) {
+static void launch_check(dpg_ctx *c, const CheckArgs &ca, int prec, cudaStream_t st) {
+  const bool fp64 = prec == DPG_FP64_STRICT;
   using R = Robot<KIND>;
   // obstacle bitmask words per lane: the fewest that cover the obstacles
   // (fewer registers), none above kMaxCullObs (no culling)
@@ -127,20 +132,23 @@ static void launch_check(dpg_ctx *c, const CheckArgs &ca, bool fp64, cudaStream_
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
     kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
   };
-  auto by_words = [&](auto real, auto band) {
+  auto by_words = [&](auto real, auto band, auto es64) {
     using Real = decltype(real);
-    constexpr bool BAND = decltype(band)::value;
+    constexpr bool BAND = decltype(band)::value, ES64 = decltype(es64)::value;
     switch (nw) {
-      case 1: go(check_pairs<KIND, Real, BAND, 1>); break;
-      case 2: go(check_pairs<KIND, Real, BAND, 2>); break;
-      case 3: go(check_pairs<KIND, Real, BAND, 3>); break;
-      case 4: go(check_pairs<KIND, Real, BAND, 4>); break;
-      default: go(check_pairs<KIND, Real, BAND, 0>); break;
+      case 1: go(check_pairs<KIND, Real, BAND, 1, ES64>); break;
+      case 2: go(check_pairs<KIND, Real, BAND, 2, ES64>); break;
+      case 3: go(check_pairs<KIND, Real, BAND, 3, ES64>); break;
+      case 4: go(check_pairs<KIND, Real, BAND, 4, ES64>); break;
+      default: go(check_pairs<KIND, Real, BAND, 0, ES64>); break;
     }
   };
-  if (fp64) by_words(0.0, std::false_type{});
-  else by_words(0.0f, std::true_type{});
+  if (fp64) by_words(0.0, std::false_type{}, std::false_type{});
+  else if (prec == DPG_FP64) by_words(0.0f, std::true_type{}, std::true_type{});
+  else by_words(0.0f, std::true_type{}, std::false_type{});
 }
+
+static bool prec_ok(int p) { return p == DPG_FP32 || p == DPG_FP64 || p == DPG_FP64_STRICT; }
 
 // primitive tiles per nn_mask block: small node batches are split over the
 // primitives too, for about two blocks per SM
@@ -608,7 +616,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   if (!c->have_prims || !c->have_env) return fail(c, DPG_ERR_STATE, "expand: upload primitives and env first");
   if (N < 0 || (N > 0 && !x)) return fail(c, DPG_ERR_ARG, "expand: bad node array");
   if (N > (int64_t)1 << 31) return fail(c, DPG_ERR_ARG, "expand: more than 2^31 nodes");
-  if (!(opts->radius >= 0) || (opts->precision != DPG_FP32 && opts->precision != DPG_FP64))
+  if (!(opts->radius >= 0) || !prec_ok(opts->precision))
     return fail(c, DPG_ERR_ARG, "expand: bad radius or precision");
   if (out->capacity < 0 || out->capacity > (int64_t)0xffffffffLL)
     return fail(c, DPG_ERR_ARG, "expand: capacity out of range");
@@ -616,12 +624,13 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   CUDA_TRY(c, cudaSetDevice(c->device));
   const int kind = c->robot.kind, nx = c->robot.nx, P = c->P;
   const int kd = key_dim(kind), od = off_dim(kind);
-  const bool fp64 = opts->precision == DPG_FP64;
+  const int prec = opts->precision;
+  const bool fp64 = prec == DPG_FP64_STRICT;  // every test in FP64
   const int64_t cap = out->capacity;
   const int64_t W = (N + 31) / 32;
   const int64_t Wpad = (W + 31) / 32 * 32;  // mask row: words of a primitive, whole emit groups
   const int64_t B = (N + kNNThreads - 1) / kNNThreads;
-  const size_t es_bytes = fp64 ? sizeof(double) : sizeof(float);
+  const size_t es_bytes = prec != DPG_FP32 ? sizeof(double) : sizeof(float);
   cudaStream_t st = c->stream;
   int rc;
   if ((rc = ensure(c, c->x64, sizeof(double) * nx * std::max<int64_t>(N, 1))) ||
@@ -817,7 +826,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       for (int j = 0; j < ca.nsub; j++) {
         ca.sub = j;
         cudaStream_t s = pipelined && (j & 1) ? c->xstream : st;
-        launch_check<KIND>(c, ca, fp64, s);
+        launch_check<KIND>(c, ca, prec, s);
         if (pipelined) cudaEventRecord(c->ev_sub[j], s);
       }
       if (pipelined) {  // join: the last launch on the second stream
@@ -906,11 +915,11 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
 // Allocation-free batched expand (dpg_expand_noalloc, declared in dpg.h).
 //
 // Who needs it: callers that must not allocate device memory at expand time
-// -- code that records the expand into a CUDA graph while a stream is being
-// captured (allocation calls are not allowed there), real-time planning loops
-// that cannot block on the device allocator, and hosts that hand all device
-// memory to their own pool.  dpg_expand may grow its per-context buffers with
-// cudaMalloc on any call; this entry point never does.
+// -- real-time planning loops that cannot block on the device allocator
+// (cudaMalloc may synchronise the device), and host programs that hand all
+// device memory to their own pool up front.  dpg_expand may grow its
+// per-context buffers with cudaMalloc on any call; this entry point never
+// does.
 //
 // Its per-call scratch (node keys and offsets, ball bitmask, per-tile counts,
 // segment bases, work-queue counters) lives in one file-scope device array of
@@ -958,7 +967,7 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
   if (N < 0 || (N > 0 && !x_dev)) return fail(c, DPG_ERR_ARG, "noalloc: bad node array");
   if (!out->node || !out->prim)
     return fail(c, DPG_ERR_ARG, "noalloc: the caller provides device arrays for node and prim");
-  if (!(opts->radius >= 0) || (opts->precision != DPG_FP32 && opts->precision != DPG_FP64))
+  if (!(opts->radius >= 0) || !prec_ok(opts->precision))
     return fail(c, DPG_ERR_ARG, "noalloc: bad radius or precision");
   if (out->capacity < 0 || out->capacity > (int64_t)0xffffffffLL)
     return fail(c, DPG_ERR_ARG, "noalloc: capacity out of range");
@@ -966,7 +975,8 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
   CUDA_TRY(c, cudaSetDevice(c->device));
   const int kind = c->robot.kind, P = c->P;
   const int kd = key_dim(kind), od = off_dim(kind);
-  const bool fp64 = opts->precision == DPG_FP64;
+  const int prec = opts->precision;
+  const bool fp64 = prec == DPG_FP64_STRICT;  // every test in FP64
   const int64_t cap = out->capacity;
   const int64_t W = (N + 31) / 32;
   const int64_t Wpad = (W + 31) / 32 * 32;
@@ -985,7 +995,7 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
   const size_t need = off_ctr + align256(sizeof(DevCounters));
   if (need > kNoAllocScratchBytes)
     return fail(c, DPG_ERR_ARG, "noalloc: N x P too large for the " + std::to_string(kNoAllocScratchBytes >> 20) +
-                                    " MiB scratch (needs " + std::to_string(need >> 20) + " MiB)");
+                                    " MiB scratch (needs " + std::to_string(need) + " bytes)");
   unsigned char *base = nullptr;
   int rc;
   if ((rc = noalloc_scratch(c, c->device, &base))) return rc;
@@ -1072,7 +1082,7 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
       nn_emit<<<(unsigned)((P * ((Wpad / 32 + kEmitGroups - 1) / kEmitGroups) + 7) / 8), 256, 0, st>>>(
           P, W, Wpad, mask, cnt, pbase, cap, po.node, po.prim);
     }
-    launch_check<KIND>(c, ca, fp64, st);
+    if (!(opts->mode & DPG_MODE_BALL_ONLY)) launch_check<KIND>(c, ca, prec, st);
     launch_err = cudaGetLastError();
   });
   if (launch_err != cudaSuccess)
@@ -1121,6 +1131,125 @@ extern "C" int dpg_mlp_node_features(dpg_ctx *c, const double *x_dev, int64_t N,
 }
 
 // ---------------------------------------------------------------------------
+// Helpers shared with lazy.cu (check_list.h).
+namespace dpg {
+
+int ctx_fail(dpg_ctx *c, int code, const std::string &msg) { return fail(c, code, msg); }
+int ctx_ensure(dpg_ctx *c, DevBuf &b, size_t bytes) { return ensure(c, b, bytes); }
+
+PrimView ctx_prim_view(dpg_ctx *c) {
+  PrimView pv{};
+  pv.P = c->P;
+  pv.S = c->S;
+  pv.len = P_<int32_t>(c->len);
+  pv.soff = P_<int64_t>(c->soff);
+  pv.order = P_<int32_t>(c->order);
+  pv.key32 = P_<float>(c->key32);
+  pv.kconst32 = P_<float>(c->kconst32);
+  pv.st64 = P_<double>(c->st64);
+  pv.st32 = P_<float>(c->st32);
+  pv.pose32 = P_<Pose<float>>(c->pose32);
+  pv.pose64 = P_<Pose<double>>(c->pose64);
+  pv.pbox = P_<double>(c->pbox);
+  pv.pbox32 = P_<float>(c->pbox32);
+  pv.coff = P_<int64_t>(c->coff);
+  pv.cbox32 = P_<float>(c->cbox32);
+  pv.tbox32 = P_<float>(c->tbox32);
+  return pv;
+}
+
+EnvView ctx_env_view(const dpg_ctx *c) {
+  EnvView ev{};
+  ev.dim = c->dim;
+  for (int i = 0; i < 3; i++) { ev.lo[i] = c->lo[i]; ev.hi[i] = c->hi[i]; }
+  ev.n_obs = c->n_obs;
+  ev.obs32 = c->obs32.p;
+  ev.obs64 = c->obs64.p;
+  return ev;
+}
+
+CheckArgs ctx_check_args(dpg_ctx *c, int prec, double contact_band, const NodeView &nv, const PairView &out) {
+  const RobotParams rp = c->rp;
+  const double band = contact_band > 0 ? contact_band : 1e-4;
+  CheckArgs ca{};
+  ca.rp = rp;
+  ca.pv = ctx_prim_view(c);
+  ca.nv = nv;
+  ca.ev = ctx_env_view(c);
+  ca.out = out;
+  ca.ord_pbase = P_<unsigned long long>(c->ord_pbase);
+  ca.ord_ibase = P_<unsigned long long>(c->ord_ibase);
+  ca.ctr = c->d_ctr;
+  ca.abort_flag = c->d_abort;
+  ca.band = prec == DPG_FP64_STRICT ? 0.0 : band;
+  ca.cull_margin = kGapCap + (float)band + 1e-3f;
+  ca.dt32 = (float)rp.dt;
+  ca.half_len32 = (float)rp.half_len;
+  ca.half_wid32 = (float)rp.half_wid;
+  ca.radius32 = (float)rp.radius;
+  ca.band32 = (float)ca.band;
+  for (int i = 0; i < 3; i++) { ca.lo32[i] = (float)c->lo[i]; ca.hi32[i] = (float)c->hi[i]; }
+  return ca;
+}
+
+void ctx_prep_nodes(dpg_ctx *c, const NodeView &nv, cudaStream_t st) {
+  if (nv.N <= 0) return;
+  with_kind(c->robot.kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    prep_nodes<KIND><<<(unsigned)((nv.N + 255) / 256), 256, 0, st>>>(nv);
+  });
+}
+
+int ctx_check_list(dpg_ctx *c, int prec, CheckArgs ca, int64_t n, const uint32_t *node_d, const uint32_t *prim_d,
+                   const uint32_t *dest_d, cudaStream_t st, bool timed) {
+  const int P = c->P;
+  int rc;
+  if ((rc = ensure(c, c->tot, sizeof(uint32_t) * P)) || (rc = ensure(c, c->q_fill, sizeof(uint32_t) * P)) ||
+      (rc = ensure(c, c->pbase, sizeof(unsigned long long) * P)) ||
+      (rc = ensure(c, c->ord_pbase, sizeof(unsigned long long) * (P + 1))) ||
+      (rc = ensure(c, c->ord_ibase, sizeof(unsigned long long) * (P + 1))) ||
+      (rc = ensure(c, c->q_sorted, 4 * (size_t)std::max<int64_t>(n, 1))) ||
+      (rc = ensure(c, c->q_idx, 4 * (size_t)std::max<int64_t>(n, 1))))
+    return rc;
+  ca.ord_pbase = P_<unsigned long long>(c->ord_pbase);
+  ca.ord_ibase = P_<unsigned long long>(c->ord_ibase);
+  ca.ctr = c->d_ctr;
+  ca.out.cap = n;
+  ca.out.node = P_<uint32_t>(c->q_sorted);
+  ca.out.prim = nullptr;
+  ca.out.out_index = P_<uint32_t>(c->q_idx);
+  ca.perm = nullptr;
+  ca.sub = 0;
+  ca.nsub = 1;
+  CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), st));
+  CUDA_TRY(c, cudaMemsetAsync(c->tot.p, 0, sizeof(uint32_t) * P, st));
+  CUDA_TRY(c, cudaMemsetAsync(c->q_fill.p, 0, sizeof(uint32_t) * P, st));
+  if (n == 0) return DPG_OK;
+  const int64_t N = ca.nv.N;
+  cudaError_t launch_err = cudaSuccess;
+  with_kind(c->robot.kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    pairs_hist<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(node_d, prim_d, n, N, P, P_<uint32_t>(c->tot), c->d_ctr);
+    scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), P_<uint32_t>(c->tot), P_<unsigned long long>(c->pbase),
+                                    P_<unsigned long long>(c->ord_pbase), P_<unsigned long long>(c->ord_ibase), n,
+                                    c->d_ctr);
+    pairs_scatter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(node_d, prim_d, n, N, P,
+                                                               P_<unsigned long long>(c->pbase),
+                                                               P_<uint32_t>(c->q_fill), P_<uint32_t>(c->q_sorted),
+                                                               P_<uint32_t>(c->q_idx), dest_d);
+    if (timed) cudaEventRecord(c->ev[2], st);
+    launch_check<KIND>(c, ca, prec, st);
+    if (timed) cudaEventRecord(c->ev[3], st);
+    launch_err = cudaGetLastError();
+  });
+  if (launch_err != cudaSuccess)
+    return fail(c, DPG_ERR_CUDA, std::string("check launch: ") + cudaGetErrorString(launch_err));
+  return DPG_OK;
+}
+
+}  // namespace dpg
+
+// ---------------------------------------------------------------------------
 // Exact check of an explicit pair list (dpg_check_pairs, dpg.h): the pairs
 // are grouped by primitive (longest first) so the same persistent warps as
 // in dpg_expand walk one primitive per warp; results go back to the input
@@ -1136,7 +1265,7 @@ extern "C" int dpg_check_pairs(dpg_ctx *c, const dpg_expand_opts *opts, int64_t 
     out->n_pairs = n;
     return fail(c, DPG_ERR_CAPACITY, "check_pairs: capacity below n");
   }
-  if (opts->precision != DPG_FP32 && opts->precision != DPG_FP64) return fail(c, DPG_ERR_ARG, "check_pairs: precision");
+  if (!prec_ok(opts->precision)) return fail(c, DPG_ERR_ARG, "check_pairs: precision");
   if (*(volatile int *)c->h_abort) return fail(c, DPG_ERR_ABORTED, "check_pairs: abort flag raised");
   CUDA_TRY(c, cudaSetDevice(c->device));
   out->n_pairs = n;
@@ -1146,23 +1275,21 @@ extern "C" int dpg_check_pairs(dpg_ctx *c, const dpg_expand_opts *opts, int64_t 
   if (n == 0) return DPG_OK;
   const int kind = c->robot.kind, nx = c->robot.nx, P = c->P;
   const int kd = key_dim(kind), od = off_dim(kind);
-  const bool fp64 = opts->precision == DPG_FP64;
-  const size_t es_bytes = fp64 ? sizeof(double) : sizeof(float);
+  const int prec = opts->precision;
+  const size_t es_bytes = prec != DPG_FP32 ? sizeof(double) : sizeof(float);
   const bool dev_in = opts->x_on_device != 0, dev_out = opts->out_on_device != 0;
   cudaStream_t st = c->stream;
   int rc;
   if ((rc = ensure(c, c->x64, sizeof(double) * nx * std::max<int64_t>(N, 1))) ||
       (rc = ensure(c, c->nkey32, sizeof(float) * kd * std::max<int64_t>(N, 1))) ||
-      (rc = ensure(c, c->noff32, sizeof(float) * od * std::max<int64_t>(N, 1))) ||
-      (rc = ensure(c, c->tot, sizeof(uint32_t) * P)) || (rc = ensure(c, c->q_fill, sizeof(uint32_t) * P)) ||
-      (rc = ensure(c, c->pbase, sizeof(unsigned long long) * P)) ||
-      (rc = ensure(c, c->ord_pbase, sizeof(unsigned long long) * (P + 1))) ||
-      (rc = ensure(c, c->ord_ibase, sizeof(unsigned long long) * (P + 1))) ||
-      (rc = ensure(c, c->q_sorted, 4 * (size_t)n)) || (rc = ensure(c, c->q_idx, 4 * (size_t)n)))
+      (rc = ensure(c, c->noff32, sizeof(float) * od * std::max<int64_t>(N, 1))))
     return rc;
   const uint32_t *node_d = node, *prim_d = prim;
   const double *x_d = x;
-  if (!dev_in) {
+  if (!dev_in) {  // host lists: reject out-of-range indices before any copy
+    for (int64_t i = 0; i < n; i++)
+      if ((int64_t)node[i] >= N || prim[i] >= (uint32_t)P)
+        return fail(c, DPG_ERR_ARG, "check_pairs: pair " + std::to_string(i) + " has node >= N or prim >= P");
     if ((rc = ensure(c, c->q_node, 4 * (size_t)n)) || (rc = ensure(c, c->q_prim, 4 * (size_t)n))) return rc;
     CUDA_TRY(c, cudaMemcpyAsync(c->x64.p, x, sizeof(double) * nx * std::max<int64_t>(N, 0), cudaMemcpyHostToDevice, st));
     CUDA_TRY(c, cudaMemcpyAsync(c->q_node.p, node, 4 * n, cudaMemcpyHostToDevice, st));
@@ -1172,10 +1299,6 @@ extern "C" int dpg_check_pairs(dpg_ctx *c, const dpg_expand_opts *opts, int64_t 
     x_d = P_<double>(c->x64);
   }
   PairView po{};
-  po.cap = n;
-  po.node = P_<uint32_t>(c->q_sorted);
-  po.prim = nullptr;
-  po.out_index = P_<uint32_t>(c->q_idx);
   if (dev_out) {
     po.verdict = out->verdict;
     po.first_invalid = out->first_invalid;
@@ -1194,74 +1317,12 @@ extern "C" int dpg_check_pairs(dpg_ctx *c, const dpg_expand_opts *opts, int64_t 
     po.min_gap = out->min_gap ? P_<float>(c->p_gap) : nullptr;
     po.flags = out->flags ? P_<uint8_t>(c->p_flags) : nullptr;
   }
-  PrimView pv{};
-  pv.P = P;
-  pv.S = c->S;
-  pv.len = P_<int32_t>(c->len);
-  pv.soff = P_<int64_t>(c->soff);
-  pv.order = P_<int32_t>(c->order);
-  pv.key32 = P_<float>(c->key32);
-  pv.kconst32 = P_<float>(c->kconst32);
-  pv.st64 = P_<double>(c->st64);
-  pv.st32 = P_<float>(c->st32);
-  pv.pose32 = P_<Pose<float>>(c->pose32);
-  pv.pose64 = P_<Pose<double>>(c->pose64);
-  pv.pbox = P_<double>(c->pbox);
-  pv.pbox32 = P_<float>(c->pbox32);
-  pv.coff = P_<int64_t>(c->coff);
-  pv.cbox32 = P_<float>(c->cbox32);
-  pv.tbox32 = P_<float>(c->tbox32);
   NodeView nv{N, x_d, P_<float>(c->nkey32), P_<float>(c->noff32)};
-  EnvView ev{};
-  ev.dim = c->dim;
-  for (int i = 0; i < 3; i++) { ev.lo[i] = c->lo[i]; ev.hi[i] = c->hi[i]; }
-  ev.n_obs = c->n_obs;
-  ev.obs32 = c->obs32.p;
-  ev.obs64 = c->obs64.p;
-  const RobotParams rp = c->rp;
-  const double band = opts->contact_band > 0 ? opts->contact_band : 1e-4;
-  CheckArgs ca{};
-  ca.rp = rp;
-  ca.pv = pv;
-  ca.nv = nv;
-  ca.ev = ev;
-  ca.out = po;
-  ca.ord_pbase = P_<unsigned long long>(c->ord_pbase);
-  ca.ord_ibase = P_<unsigned long long>(c->ord_ibase);
-  ca.ctr = c->d_ctr;
-  ca.abort_flag = c->d_abort;
-  ca.band = fp64 ? 0.0 : band;
-  ca.cull_margin = kGapCap + (float)band + 1e-3f;
-  ca.dt32 = (float)rp.dt;
-  ca.half_len32 = (float)rp.half_len;
-  ca.half_wid32 = (float)rp.half_wid;
-  ca.radius32 = (float)rp.radius;
-  ca.band32 = (float)ca.band;
-  for (int i = 0; i < 3; i++) { ca.lo32[i] = (float)c->lo[i]; ca.hi32[i] = (float)c->hi[i]; }
+  const CheckArgs ca = ctx_check_args(c, prec, opts->contact_band, nv, po);
 
   CUDA_TRY(c, cudaEventRecord(c->ev[1], st));
-  CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), st));
-  CUDA_TRY(c, cudaMemsetAsync(c->tot.p, 0, sizeof(uint32_t) * P, st));
-  CUDA_TRY(c, cudaMemsetAsync(c->q_fill.p, 0, sizeof(uint32_t) * P, st));
-  cudaError_t launch_err = cudaSuccess;
-  with_kind(kind, [&](auto K) {
-    constexpr int KIND = decltype(K)::value;
-    using R = Robot<KIND>;
-    if (N > 0) prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
-    pairs_hist<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(prim_d, n, P_<uint32_t>(c->tot));
-    scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), P_<uint32_t>(c->tot), P_<unsigned long long>(c->pbase),
-                                    P_<unsigned long long>(c->ord_pbase), P_<unsigned long long>(c->ord_ibase), n,
-                                    c->d_ctr);
-    pairs_scatter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(node_d, prim_d, n, P_<unsigned long long>(c->pbase),
-                                                               P_<uint32_t>(c->q_fill), P_<uint32_t>(c->q_sorted),
-                                                               P_<uint32_t>(c->q_idx));
-    cudaEventRecord(c->ev[2], st);
-    launch_check<KIND>(c, ca, fp64, st);
-    cudaEventRecord(c->ev[3], st);
-    launch_err = cudaGetLastError();
-  });
-  if (launch_err != cudaSuccess)
-    return fail(c, DPG_ERR_CUDA, std::string("check_pairs launch: ") + cudaGetErrorString(launch_err));
+  ctx_prep_nodes(c, nv, st);
+  if ((rc = ctx_check_list(c, prec, ca, n, node_d, prim_d, nullptr, st, true)) != DPG_OK) return rc;
   CUDA_TRY(c, cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
   if (!dev_out) {
     struct { void *dst; void *src; size_t b; } cp[] = {
@@ -1273,6 +1334,9 @@ extern "C" int dpg_check_pairs(dpg_ctx *c, const dpg_expand_opts *opts, int64_t 
   CUDA_TRY(c, cudaStreamSynchronize(st));
   const DevCounters h = *c->h_ctr;
   out->n_contact_recheck = (int64_t)h.n_recheck;
+  if (h.n_bad)
+    return fail(c, DPG_ERR_ARG, "check_pairs: " + std::to_string(h.n_bad) +
+                                    " pairs have node >= N or prim >= P (left unchecked)");
   if (h.status == DPG_ERR_ABORTED) return fail(c, DPG_ERR_ABORTED, "check_pairs: aborted");
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);

@@ -50,7 +50,7 @@ struct DevCounters {
   unsigned long long n_ball_recheck;
   unsigned long long n_overflow;
   int status;  // 0 ok, DPG_ERR_ABORTED
-  int pad;
+  unsigned n_bad;  // dpg_check_pairs: pairs whose node or primitive index is out of range
 };
 
 template <class Real> struct __align__(sizeof(Real) * 4) Pose { Real cx, cy, c, s; };
@@ -717,22 +717,34 @@ __global__ void build_chunks(RobotParams rp, int P, const int32_t *len, const in
 namespace dpg {
 
 // ---- explicit pair lists (dpg_check_pairs): group pairs by primitive -----
-static __global__ void pairs_hist(const uint32_t *prim, int64_t n, uint32_t *hist) {
+// Pairs with node >= N or prim >= P (caller-supplied device lists) are
+// counted in ctr->n_bad and left out of every table; the call then fails.
+static __global__ void pairs_hist(const uint32_t *node, const uint32_t *prim, int64_t n, int64_t N, int P,
+                                  uint32_t *hist, DevCounters *ctr) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) atomicAdd(&hist[prim[i]], 1u);
+  if (i >= n) return;
+  const uint32_t p = prim[i];
+  if (p >= (uint32_t)P || (int64_t)node[i] >= N) {
+    atomicAdd(&ctr->n_bad, 1u);
+    return;
+  }
+  atomicAdd(&hist[p], 1u);
 }
 
 // position of pair i inside its primitive's segment (order within a segment
 // is arbitrary; results are written back at the input positions)
-static __global__ void pairs_scatter(const uint32_t *node, const uint32_t *prim, int64_t n,
+// sorted_idx receives the output row of each pair: dest[i] when given (the
+// lazy rounds write into the rows of the whole candidate list), else i.
+static __global__ void pairs_scatter(const uint32_t *node, const uint32_t *prim, int64_t n, int64_t N, int P,
                                      const unsigned long long *pbase, uint32_t *fill, uint32_t *sorted_node,
-                                     uint32_t *sorted_idx) {
+                                     uint32_t *sorted_idx, const uint32_t *dest) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t p = prim[i];
+  if (p >= (uint32_t)P || (int64_t)node[i] >= N) return;  // counted by pairs_hist
   const unsigned long long pos = pbase[p] + atomicAdd(&fill[p], 1u);
   sorted_node[pos] = node[i];
-  sorted_idx[pos] = (uint32_t)i;
+  sorted_idx[pos] = dest ? dest[i] : (uint32_t)i;
 }
 
 }  // namespace dpg

@@ -137,7 +137,7 @@ class Context:
         node = np.ascontiguousarray(node, dtype=np.uint32)
         prim = np.ascontiguousarray(prim, dtype=np.uint32)
         n = len(node)
-        es_dtype = np.float64 if precision == 1 else np.float32
+        es_dtype = np.float64 if precision != 0 else np.float32
         o = dict(verdict=np.empty(n, np.uint8), first_invalid=np.empty(n, np.int16),
                  end_state=np.empty((n, self.nx), es_dtype), min_gap=np.empty(n, np.float32),
                  flags=np.empty(n, np.uint8))
@@ -164,7 +164,7 @@ class Context:
         opts = ExpandOpts(radius=radius, precision=precision, x_on_device=0, out_on_device=0,
                           mode=1 if ball_only else 0, contact_band=contact_band, ball_band=ball_band)
         while True:
-            es_dtype = np.float64 if precision == 1 else np.float32
+            es_dtype = np.float64 if precision != 0 else np.float32
             o = outputs if outputs is not None else dict(
                 node=np.empty(capacity, np.uint32), prim=np.empty(capacity, np.uint32),
                 verdict=np.empty(capacity, np.uint8), first_invalid=np.empty(capacity, np.int16),

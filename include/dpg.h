@@ -29,12 +29,15 @@
  *   - Input arrays are copied; the caller keeps ownership.  Output arrays
  *     are owned by the caller (host or device memory, see dpg_expand_opts).
  *   - Precision: DPG_FP32 computes rollouts and separating-axis tests in
- *     FP32 and recomputes in FP64, on the GPU, every pair whose gap or
- *     bounds margin lies within contact_band of zero; DPG_FP64 computes the
- *     transforms, bounds and collision tests and the end states in FP64.
- *     In both modes the ball test runs in FP32 and is decided in FP64 when
- *     the distance lies within ball_band of the radius, so the neighbour
- *     sets are those of an FP64 test.
+ *     FP32 and recomputes in FP64, on the GPU, every test whose gap or
+ *     bounds margin lies within contact_band of zero, so verdicts and first
+ *     invalid states are those of FP64 tests; end states are FP32.
+ *     DPG_FP64 runs the same tests and writes the end states in FP64 (the
+ *     FP64 canonical state plus the FP64 node offset).  DPG_FP64_STRICT
+ *     computes every transform, bounds and collision test in FP64 (1/64 of
+ *     the FP32 rate on this GPU).  In every mode the ball test runs in FP32
+ *     and is decided in FP64 when the distance lies within ball_band of the
+ *     radius, so the neighbour sets are those of an FP64 test.
  */
 #ifndef DPG_H
 #define DPG_H
@@ -71,8 +74,9 @@ extern "C" {
 #define DPG_OUT_OF_BOUNDS 2
 
 /* precision */
-#define DPG_FP32 0
-#define DPG_FP64 1
+#define DPG_FP32 0        /* FP32 tests, FP64 decisions in the bands, FP32 end states */
+#define DPG_FP64 1        /* the same tests and decisions, end states in FP64 */
+#define DPG_FP64_STRICT 2 /* every transform, bounds and collision test in FP64 */
 
 /* dpg_expand_opts.mode */
 #define DPG_MODE_BALL_ONLY 1
@@ -103,7 +107,7 @@ typedef struct dpg_robot_desc {
 
 typedef struct dpg_expand_opts {
   double radius;          /* ball radius = alpha * delta (dbastar.cpp:585-586) */
-  int32_t precision;      /* DPG_FP32 or DPG_FP64 */
+  int32_t precision;      /* DPG_FP32, DPG_FP64 or DPG_FP64_STRICT */
   int32_t x_on_device;    /* x is a device pointer */
   int32_t out_on_device;  /* output arrays are device pointers */
   int32_t mode;           /* 0: full expand; DPG_MODE_BALL_ONLY: in-ball pairs only
@@ -126,7 +130,7 @@ typedef struct dpg_expand_out {
   uint32_t *prim;          /* primitive index (upload order = Motion::idx) */
   uint8_t *verdict;        /* DPG_VALID / DPG_COLLISION / DPG_OUT_OF_BOUNDS */
   int16_t *first_invalid;  /* first out-of-bounds or colliding state, or L */
-  void *end_state;         /* n_pairs x nx, float (DPG_FP32) or double (DPG_FP64) */
+  void *end_state;         /* n_pairs x nx, float (DPG_FP32) or double (DPG_FP64, _STRICT) */
   float *min_gap;          /* min axis-aligned clearance along the checked states */
   uint8_t *flags;          /* DPG_FLAG_* */
   /* counters (out) */
@@ -193,24 +197,32 @@ int dpg_check_pairs(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const 
 
 /* Allocation-free form of dpg_expand.  No counterpart in the reference (its
  * expansion runs on the host).  For callers that cannot allocate device
- * memory at expand time: code capturing a CUDA graph, real-time planning
- * loops that must not block on the allocator, hosts that give all device
- * memory to their own pool.  dpg_expand may call cudaMalloc to grow its
+ * memory while they expand: real-time planning loops that must not block
+ * on the device allocator (cudaMalloc can synchronise the device and take
+ * milliseconds), and host programs that hand all device memory to their
+ * own pool up front, so a cudaMalloc inside the library would fail or
+ * break their accounting.  dpg_expand may call cudaMalloc to grow its
  * buffers; this call never allocates: its per-call scratch is one 64 MiB
  * file-scope device array that every GPU loading the library holds until
- * exit.
+ * the process exits.
  *   - x_dev (N x nx doubles) and every array in `out` are DEVICE pointers;
  *     out->node and out->prim are required.  opts->x_on_device and
  *     opts->out_on_device are ignored (both are device).
- *   - The scratch must hold 4*(KEYD+offset_dim)*N + 4*ceil(N/32)*ceil32(P)
- *     + 4*ceil(N/256)*P + ~28*P bytes (rounded up per buffer); larger N x P is
- *     rejected with DPG_ERR_ARG and a message.  About 60,000 car1 nodes x
- *     5,000 primitives fit.
+ *   - The scratch must hold, with each term rounded up to 256 bytes,
+ *     4*KEYD*N + 4*OFFD*N + 4*ceil32(ceil(N/32))*P + 4*ceil(N/256)*P + 28*P
+ *     bytes (KEYD, OFFD: key and offset components of the robot: unicycle1
+ *     1, 2; car1 2, 2; quad2d 2, 4; quadrotor 7, 6; ceil32 rounds up to a
+ *     multiple of 32).  About 92,000 car1 nodes x 5,000 primitives fit;
+ *     larger N x P is rejected with DPG_ERR_ARG and a message that gives
+ *     the need.
  *   - All calls share the array, which keeps the last call's contents; the
- *     call clears its counters itself.  Calls whose device work overlaps
- *     (other streams or host threads) race on it: serialise them.
- *   - The first call on a device looks the array up (cudaGetSymbolAddress);
- *     make that first call before any stream capture.
+ *     call clears what must start at zero itself.  Calls whose device work
+ *     overlaps (other streams, other host threads, other contexts on the
+ *     same GPU) race on it: serialise them.
+ *   - The first call on a device looks the array's device address up
+ *     (cudaGetSymbolAddress, with that device current); make that first
+ *     call before any stream capture.
+ *   - It honours DPG_MODE_BALL_ONLY; it does not update dpg_last_timings.
  * Results are identical to dpg_expand's with device outputs. */
 int dpg_expand_noalloc(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x_dev,
                        dpg_expand_out *out);

@@ -159,7 +159,7 @@ class Expander {
     for (;;) {
       node_.resize(cap); prim_.resize(cap); verdict_.resize(cap); fi_.resize(cap); gap_.resize(cap); flags_.resize(cap);
       es32_.resize(precision == DPG_FP32 ? cap * nx : 0);
-      es64_.resize(precision == DPG_FP64 ? cap * nx : 0);
+      es64_.resize(precision != DPG_FP32 ? cap * nx : 0);
       r = dpg_expand_out{};
       r.capacity = cap;
       r.node = node_.data(); r.prim = prim_.data(); r.verdict = verdict_.data(); r.first_invalid = fi_.data();

@@ -1,7 +1,8 @@
 """Generate the golden fixtures in this directory.
 
-Reads the reference's own data (the dynoplan checkout passed as argv[1],
-default /root/reference) and writes small JSON fixtures; it also records the
+Reads the reference's own data (the dynoplan checkout, a required
+argument: ``python make_golden.py <dynoplan checkout>``) and writes small
+JSON fixtures; it also records the
 oracle's outputs on small seeded workloads.  Run it where the reference is
 present; the fixtures it writes are committed and the tests only read them.
 
@@ -123,4 +124,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <path of the dynoplan checkout>")
+    main(sys.argv[1])

@@ -2,10 +2,13 @@
 
 Bars (the tolerances every parity test states):
   pairs, verdicts, first_invalid   identical
-  end states                      FP64 path: 1e-9 absolute; FP32 path:
-                                  1e-5 relative (|d| <= 1e-5 * max(1, |x|));
-                                  wrapped angles compared modulo 2 pi
-  min_gap (FP32 output)           FP64 path: 1e-5; FP32 path: 2e-4 absolute
+  end states                      DPG_FP64 and DPG_FP64_STRICT: 1e-9
+                                  absolute; DPG_FP32: 1e-5 relative
+                                  (|d| <= 1e-5 * max(1, |x|)); wrapped angles
+                                  compared modulo 2 pi
+  min_gap (FP32 output)           DPG_FP64_STRICT (FP64 tests): 1e-5;
+                                  DPG_FP32 and DPG_FP64 (FP32 tests): 2e-4
+                                  absolute
 """
 import math
 
@@ -38,7 +41,7 @@ def compare(kind, gpu, ora, precision, min_gap=True):
     d = ge - oe
     for c in ANGLE_COMPS[kind]:
         d[:, c] = (d[:, c] + math.pi) % (2 * math.pi) - math.pi
-    if precision == 1:
+    if precision != 0:   # DPG_FP64, DPG_FP64_STRICT: FP64 end states
         tol = np.full_like(oe, 1e-9)
     else:
         tol = 1e-5 * np.maximum(1.0, np.abs(oe))
@@ -46,7 +49,7 @@ def compare(kind, gpu, ora, precision, min_gap=True):
     assert not bad.any(), f"end state mismatch at {np.argwhere(bad)[:5].tolist()}: max {np.abs(d).max()}"
     out = {"end_state_max_abs": float(np.abs(d).max()) if len(d) else 0.0}
     if min_gap and len(d):
-        tol = 1e-5 if precision == 1 else 2e-4
+        tol = 1e-5 if precision == 2 else 2e-4   # FP64 tests only in DPG_FP64_STRICT
         gg, og = g["min_gap"].astype(np.float64), o["min_gap"]
         # NaN (out of bounds) on the same rows
         np.testing.assert_array_equal(np.isnan(gg), np.isnan(og))
@@ -54,8 +57,9 @@ def compare(kind, gpu, ora, precision, min_gap=True):
         # may fall on either side
         near_cap = lambda v: np.isinf(v) | (v >= GAP_CAP - tol)
         both = np.isfinite(gg) & np.isfinite(og)
-        ok =np.where(np.isnan(og), True,
-                      np.where(both, np.abs(gg - og) <= tol, near_cap(gg) & near_cap(og)))
+        close = np.zeros(len(gg), bool)
+        close[both] = np.abs(gg[both] - og[both]) <= tol      # differences of finite rows only
+        ok = np.where(np.isnan(og), True, np.where(both, close, near_cap(gg) & near_cap(og)))
         assert ok.all(), f"min_gap mismatch at {np.argwhere(~ok)[:5].ravel().tolist()}"
         out["min_gap_max_abs"] = float(np.abs(gg[both] - og[both]).max(initial=0))
     return out

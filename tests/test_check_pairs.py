@@ -66,3 +66,45 @@ def test_check_pairs_matches_oracle(gpu, cfg, scale, precision):
     # ball-only mode gives exactly the oracle's pair set
     key = lambda n, q: np.sort(n.astype(np.int64) * (1 << 32) + q.astype(np.int64))
     np.testing.assert_array_equal(key(ball["node"], ball["prim"]), key(ora["node"], ora["prim"]))
+
+
+def test_check_pairs_rejects_out_of_range_indices(gpu):
+    """A node index >= N or a primitive index >= P is refused with
+    DPG_ERR_ARG: host lists before any copy, device lists by the kernels
+    that group the pairs (they skip such pairs and count them); the in-range
+    pairs of the same call are untouched memory-wise, and the context stays
+    usable."""
+    import ctypes as C
+
+    import torch
+
+    from dynoplan_gb300 import _lib
+    wl = W.make_workload(2, scale=0.01, seed=77)
+    N, P = len(wl.nodes), wl.prims.P
+    good_n = np.arange(8, dtype=np.uint32) % N
+    good_p = np.arange(8, dtype=np.uint32) % P
+    with gpu.Context(wl.robot) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        for bad_n, bad_p in ((N, 0), (0, P), (2 ** 31, 2 ** 32 - 1)):
+            node = np.r_[good_n, np.uint32(bad_n)].astype(np.uint32)
+            prim = np.r_[good_p, np.uint32(bad_p)].astype(np.uint32)
+            with pytest.raises(_lib.DpgError) as e:
+                ctx.check_pairs(wl.nodes, node, prim)
+            assert e.value.code == _lib.DPG_ERR_ARG
+            # the same lists in device memory
+            x_d = torch.from_numpy(wl.nodes).cuda()
+            n_d = torch.from_numpy(node.view(np.int32)).cuda()
+            p_d = torch.from_numpy(prim.view(np.int32)).cuda()
+            verdict = torch.zeros(len(node), dtype=torch.uint8, device="cuda")
+            opts = _lib.ExpandOpts(radius=0.0, precision=0, x_on_device=1, out_on_device=1, mode=0,
+                                   contact_band=1e-4, ball_band=1e-5)
+            out = _lib.ExpandOut(capacity=len(node))
+            out.verdict = C.c_void_p(verdict.data_ptr())
+            torch.cuda.synchronize()
+            rc = ctx.lib.dpg_check_pairs(ctx.h, C.byref(opts), N, C.c_void_p(x_d.data_ptr()), len(node),
+                                         C.c_void_p(n_d.data_ptr()), C.c_void_p(p_d.data_ptr()), C.byref(out))
+            assert rc == _lib.DPG_ERR_ARG
+        # still usable, and the good pairs agree with a clean call
+        ok = ctx.check_pairs(wl.nodes, good_n, good_p)
+        assert ok["n_pairs"] == 8

@@ -1,10 +1,10 @@
 """dpg_expand_noalloc, the allocation-free expand (include/dpg.h).
 
-Callers that cannot allocate device memory while they expand -- code
-capturing a CUDA graph, real-time planning loops that must not block on the
-device allocator, hosts that hand all device memory to their own pool -- use
-this entry point; its scratch is a fixed 64 MiB device array inside the
-library instead of buffers it grows with cudaMalloc.  This file checks,
+Callers that cannot allocate device memory while they expand -- real-time
+planning loops that must not block on the device allocator, host programs
+that hand all device memory to their own pool up front -- use this entry
+point; its scratch is a fixed 64 MiB device array inside the library instead
+of buffers it grows with cudaMalloc.  This file checks,
 through the C ABI, that two calls in a row give the results of the regular
 entry point (same tolerance as the other parity tests), that device memory
 does not change across the calls, and that a batch too large for the
@@ -87,18 +87,34 @@ def test_noalloc_matches_expand_twice(dpg_lib, cfg, scale, precision):
         assert torch.cuda.mem_get_info()[0] == free_before   # nothing was allocated
 
 
+def _scratch_need(N, P, keyd, offd):
+    """bytes of scratch a call needs: the formula of include/dpg.h"""
+    a = lambda v: (v + 255) // 256 * 256
+    W = (N + 31) // 32
+    Wpad = (W + 31) // 32 * 32
+    B = (N + 255) // 256
+    return (a(4 * keyd * N) + a(4 * offd * N) + a(4 * Wpad * P) + a(4 * B * P) + a(4 * P) + a(8 * P)
+            + 2 * a(8 * (P + 1)) + a(112))
+
+
 def test_noalloc_refuses_batches_beyond_its_scratch(dpg_lib):
     torch = pytest.importorskip("torch")
+    import re
+
     from dynoplan_gb300 import _lib
     from dynoplan_gb300 import gpu as G
     wl = W.make_workload(2, scale=0.01, seed=77)
+    N, P = 100_000, 5000
+    assert _scratch_need(92_000, P, 2, 2) <= 64 << 20 < _scratch_need(N, P, 2, 2)
     with G.Context(wl.robot) as ctx:
-        ctx.upload_primitives(W.make_primitives(wl.robot, 5000, 5, 10, seed=3))
+        ctx.upload_primitives(W.make_primitives(wl.robot, P, 5, 10, seed=3))
         ctx.upload_env(wl.env)
-        x_d = torch.zeros((8, wl.robot.nx), dtype=torch.float64, device="cuda:0")
+        # x holds all N rows, so that a call that went ahead would still read
+        # inside it; the refusal comes on the host before any launch
+        x_d = torch.from_numpy(W.make_nodes(wl.robot, wl.env, N, seed=5)).to("cuda:0")
         outs = _device_out(torch, 16, wl.robot.nx, 0)
-        # 200,000 nodes x 5,000 primitives needs > 64 MiB: refused on the host
-        # before any kernel reads x
-        rc, _ = _call(dpg_lib, ctx, x_d, 200_000, outs, 16, wl.radius, 0)
+        rc, _ = _call(dpg_lib, ctx, x_d, N, outs, 16, wl.radius, 0)
         assert rc == _lib.DPG_ERR_ARG
-        assert b"MiB" in dpg_lib.dpg_last_error(ctx.h)
+        msg = dpg_lib.dpg_last_error(ctx.h).decode()
+        need = int(re.search(r"needs (\d+) bytes", msg).group(1))
+        assert need == _scratch_need(N, P, 2, 2), msg   # the header's formula
