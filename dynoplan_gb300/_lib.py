@@ -22,6 +22,8 @@ DPG_ERR_ABORTED = -5
 DPG_ERR_CAPACITY = -6
 DPG_ERR_STATE = -7
 DPG_ERR_NODEVICE = -8
+DPG_UNCHECKED = 255
+DPG_FLAG_ACCEPTED = 2
 
 DPG_FP32 = 0
 DPG_FP64 = 1
@@ -44,6 +46,11 @@ class ExpandOpts(C.Structure):
         ("out_on_device", C.c_int32), ("mode", C.c_int32),
         ("contact_band", C.c_double), ("ball_band", C.c_double),
     ]
+
+
+class LazyStats(C.Structure):
+    _fields_ = [("n_checked", C.c_int64), ("n_valid", C.c_int64), ("n_accepted", C.c_int64),
+                ("rounds", C.c_int32), ("max_candidates", C.c_int32)]
 
 
 class ExpandOut(C.Structure):
@@ -74,6 +81,9 @@ SIGNATURES = [
                                      C.POINTER(ExpandOut)]),
     ("dpg_check_pairs", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p, C.c_int64,
                                   C.c_void_p, C.c_void_p, C.POINTER(ExpandOut)]),
+    ("dpg_lazy_check", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p, C.c_int64,
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(ExpandOut),
+                                 C.POINTER(LazyStats)]),
     ("dpg_sync", C.c_int, [C.c_void_p]),
     ("dpg_set_abort", C.c_int, [C.c_void_p, C.c_int32]),
     ("dpg_host_alloc", C.c_void_p, [C.c_size_t]),
@@ -118,6 +128,8 @@ SIGNATURES = [
     # include/dpg_bench.h
     ("dpg_bench_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("dpg_bench_flush_l2", C.c_int, [C.c_int, C.c_size_t]),
+    ("dpg_bench_per_node_expand", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_int32, C.c_void_p,
+                                            C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
 ]
 
 _lib = None

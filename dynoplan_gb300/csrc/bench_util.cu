@@ -1,6 +1,9 @@
 // bench_util.cu -- measurement helpers of include/dpg_bench.h.
 #include <cuda_runtime.h>
 
+#include <chrono>
+#include <vector>
+
 #include "dpg.h"
 #include "dpg_bench.h"
 
@@ -62,4 +65,63 @@ extern "C" int dpg_bench_flush_l2(int device, size_t bytes) {
   }
   cudaMemsetAsync(buf, (int)(bytes & 0xff), bytes, 0);
   return cudaDeviceSynchronize() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+extern "C" int dpg_bench_per_node_expand(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t n_nodes, int32_t nx,
+                                         const double *x, int64_t *pairs, double *seconds) {
+  if (!ctx || !opts || !x || !pairs || !seconds || n_nodes < 0 || nx < 1) return DPG_ERR_ARG;
+  dpg_expand_opts o = *opts;
+  o.x_on_device = 0;
+  o.out_on_device = 0;
+  int64_t cap = 0;
+  void *buf[7] = {};
+  auto release = [&]() {
+    for (void *&p : buf) {
+      dpg_host_free(p);
+      p = nullptr;
+    }
+  };
+  auto grow = [&](int64_t rows) -> bool {
+    release();
+    const size_t sz[7] = {4, 4, 1, 2, (size_t)8 * nx, 4, 1};
+    for (int i = 0; i < 7; i++)
+      if (!(buf[i] = dpg_host_alloc(sz[i] * (size_t)rows))) return false;
+    cap = rows;
+    return true;
+  };
+  if (!grow(1 << 14)) {
+    release();
+    return DPG_ERR_OOM;
+  }
+  int64_t total = 0;
+  int rc = DPG_OK;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (int64_t i = 0; i < n_nodes && rc == DPG_OK; i++) {
+    for (;;) {
+      dpg_expand_out out{};
+      out.capacity = cap;
+      out.node = (uint32_t *)buf[0];
+      out.prim = (uint32_t *)buf[1];
+      out.verdict = (uint8_t *)buf[2];
+      out.first_invalid = (int16_t *)buf[3];
+      out.end_state = buf[4];
+      out.min_gap = (float *)buf[5];
+      out.flags = (uint8_t *)buf[6];
+      rc = dpg_expand(ctx, &o, 1, x + i * nx, &out);
+      if (rc == DPG_ERR_CAPACITY) {
+        if (!grow(out.n_pairs)) {
+          rc = DPG_ERR_OOM;
+          break;
+        }
+        continue;
+      }
+      if (rc == DPG_OK) total += out.n_pairs;
+      break;
+    }
+  }
+  const auto t1 = std::chrono::steady_clock::now();
+  release();
+  *pairs = total;
+  *seconds = std::chrono::duration<double>(t1 - t0).count();
+  return rc;
 }

@@ -58,6 +58,9 @@ struct dpg_ctx {
   cudaEvent_t ev_tot = nullptr;
   unsigned long long *h_bases = nullptr;  // [2][h_bases_n]: ord_ibase, ord_pbase
   size_t h_bases_n = 0;
+  // dpg_lazy_check: candidates by node, ranks, cursors, round lists, counters
+  DevBuf lz_off, lz_cnt, lz_cur, lz_next, lz_valid, lz_rank, lz_lnode, lz_lprim, lz_ldest, lz_ctr;
+  void *h_lz = nullptr;  // pinned mirror of the lazy counters
   int *h_abort = nullptr;             // mapped pinned
   int *d_abort = nullptr;
   cudaEvent_t ev[6] = {};

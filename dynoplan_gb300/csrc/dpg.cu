@@ -314,11 +314,13 @@ void dpg_destroy(dpg_ctx *c) {
                     &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32,
                     &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill,
                     &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_rank, &c->ord_tiles, &c->x64s,
-                    &c->kg_start, &c->kg_tab};
+                    &c->kg_start, &c->kg_tab, &c->lz_off, &c->lz_cnt, &c->lz_cur, &c->lz_next, &c->lz_valid,
+                    &c->lz_rank, &c->lz_lnode, &c->lz_lprim, &c->lz_ldest, &c->lz_ctr};
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
   if (c->h_bases) cudaFreeHost(c->h_bases);
+  if (c->h_lz) cudaFreeHost(c->h_lz);
   for (auto &e : c->ev_sub)
     if (e) cudaEventDestroy(e);
   if (c->ev_tot) cudaEventDestroy(c->ev_tot);
@@ -696,6 +698,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     }
     if (c->h_bases_n < (size_t)P + 1) {
       if (c->h_bases) cudaFreeHost(c->h_bases);
+  if (c->h_lz) cudaFreeHost(c->h_lz);
       c->h_bases = nullptr;
       c->h_bases_n = 0;
       CUDA_TRY(c, cudaHostAlloc(&c->h_bases, 2 * sizeof(unsigned long long) * (P + 1), cudaHostAllocDefault));

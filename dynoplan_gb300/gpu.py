@@ -8,7 +8,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import ExpandOpts, ExpandOut, RobotDesc, check
+from ._lib import ExpandOpts, ExpandOut, LazyStats, RobotDesc, check
 
 VALID, COLLISION, OUT_OF_BOUNDS = 0, 1, 2
 
@@ -188,17 +188,40 @@ class Context:
         return res
 
     def expand_device(self, x_ptr: int, N: int, radius: float, out_ptrs: dict, capacity: int,
-                      precision: int = 0, contact_band: float = 1e-4, ball_band: float = 1e-5):
+                      precision: int = 0, contact_band: float = 1e-4, ball_band: float = 1e-5,
+                      ball_only: bool = False):
         """Expand with the nodes and all outputs in device memory (raw device
-        pointers); returns the counters."""
+        pointers); returns the counters.  ball_only: the in-ball pairs
+        (node, prim) only."""
         opts = ExpandOpts(radius=radius, precision=precision, x_on_device=1, out_on_device=1,
-                          mode=0, contact_band=contact_band, ball_band=ball_band)
+                          mode=1 if ball_only else 0, contact_band=contact_band, ball_band=ball_band)
         out = ExpandOut(capacity=capacity)
         for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap", "flags"):
             setattr(out, k, C.c_void_p(out_ptrs[k]) if out_ptrs.get(k) else None)
         check(self.lib.dpg_expand(self.h, C.byref(opts), N, C.c_void_p(x_ptr), C.byref(out)), self.h)
         return dict(n_pairs=int(out.n_pairs), n_scanned=int(out.n_scanned),
                     n_contact_recheck=int(out.n_contact_recheck), n_ball_recheck=int(out.n_ball_recheck))
+
+    def lazy_check_device(self, x_ptr: int, N: int, n: int, node_ptr: int, prim_ptr: int, out_ptrs: dict,
+                          limit: int, score_ptr: int | None = None, score_stride: int = 1, precision: int = 0,
+                          contact_band: float = 1e-4) -> dict:
+        """dpg_lazy_check on device arrays: the n candidates (node, prim) of
+        the N nodes, ranked per node by score (ascending; None = motion
+        order), exact-checked in rank order until each node has `limit`
+        valid motions.  out_ptrs: device arrays of n rows (verdict and
+        flags required).  Returns the lazy statistics."""
+        opts = ExpandOpts(radius=0.0, precision=precision, x_on_device=1, out_on_device=1, mode=0,
+                          contact_band=contact_band, ball_band=1e-5)
+        out = ExpandOut(capacity=n)
+        for k in ("verdict", "first_invalid", "end_state", "min_gap", "flags"):
+            setattr(out, k, C.c_void_p(out_ptrs[k]) if out_ptrs.get(k) else None)
+        st = LazyStats()
+        check(self.lib.dpg_lazy_check(self.h, C.byref(opts), N, C.c_void_p(x_ptr), n, C.c_void_p(node_ptr),
+                                      C.c_void_p(prim_ptr), C.c_void_p(score_ptr) if score_ptr else None,
+                                      score_stride, limit, C.byref(out), C.byref(st)), self.h)
+        return dict(n_checked=int(st.n_checked), n_valid=int(st.n_valid), n_accepted=int(st.n_accepted),
+                    rounds=int(st.rounds), max_candidates=int(st.max_candidates),
+                    n_contact_recheck=int(out.n_contact_recheck))
 
     def timings(self):
         t = (C.c_double * 4)()

@@ -72,6 +72,7 @@ extern "C" {
 #define DPG_VALID 0
 #define DPG_COLLISION 1
 #define DPG_OUT_OF_BOUNDS 2
+#define DPG_UNCHECKED 255 /* dpg_lazy_check: candidate never checked */
 
 /* precision */
 #define DPG_FP32 0        /* FP32 tests, FP64 decisions in the bands, FP32 end states */
@@ -83,6 +84,7 @@ extern "C" {
 
 /* per-pair flags */
 #define DPG_FLAG_CONTACT_RECHECK 1 /* verdict recomputed in FP64 (contact/bounds band) */
+#define DPG_FLAG_ACCEPTED 2        /* dpg_lazy_check: among the node's first `limit` valid motions */
 
 /* Robot description: the subset of dynobench::Model_robot the expansion uses
  * (nx, nu, ref_dt, distance_weights, collision geometry, dynamics
@@ -194,6 +196,45 @@ int dpg_expand(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const doubl
  * out->capacity must be >= n (out->node / out->prim are not written). */
 int dpg_check_pairs(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x, int64_t n,
                     const uint32_t *node, const uint32_t *prim, dpg_expand_out *out);
+
+/* Lazy exact check of candidate pairs, a batch of nodes at a time: the
+ * check loop of the search, src/dbastar/dbastar.cpp:809-919, which walks a
+ * node's neighbours (Expander::expand_lazy, dbastar.hpp:270-312) in order,
+ * exact-checks each (check_lazy_trajectory, dbastar.cpp:391-490) and stops
+ * once limit_branching_factor motions were taken (:916-918).
+ *   - The n candidates (node_dev[i], prim_dev[i]) -- e.g. the pairs of a
+ *     DPG_MODE_BALL_ONLY expand -- are ranked per node by ascending
+ *     score_dev[i * score_stride] (NaN last), ties by ascending primitive
+ *     index; score_dev NULL ranks by primitive index (motion order).  A
+ *     surrogate's collision logit (dpg_mlp_forward, stride 2) puts the
+ *     likely-valid motions first.
+ *   - Candidates are exact-checked in rank order, in rounds, until every
+ *     node has `limit` valid motions or no candidate left.  The first
+ *     `limit` valid candidates of each node in rank order get
+ *     DPG_FLAG_ACCEPTED; every accepted motion is exact-checked.
+ *   - All pointers are DEVICE pointers (x_dev N x nx doubles).  out's arrays
+ *     have a row per candidate (capacity >= n); verdict and flags are
+ *     required, the others optional.  Unchecked candidates get verdict
+ *     DPG_UNCHECKED; a checked one gets the verdict, first invalid state,
+ *     end state and min_gap dpg_check_pairs gives it.  out->node and
+ *     out->prim are not used.
+ *   - A node may have at most 16384 candidates (DPG_ERR_CAPACITY beyond);
+ *     an out-of-range index gives DPG_ERR_ARG.
+ *   - stats (may be NULL) receives the counts of checked, valid and
+ *     accepted candidates and the number of rounds.
+ * No counterpart in the reference as a batch call; per node it takes the
+ * same motions as the reference loop would for that neighbour order. */
+typedef struct dpg_lazy_stats {
+  int64_t n_checked;       /* candidates exact-checked */
+  int64_t n_valid;         /* of those, DPG_VALID */
+  int64_t n_accepted;      /* candidates with DPG_FLAG_ACCEPTED */
+  int32_t rounds;          /* check rounds run */
+  int32_t max_candidates;  /* the largest candidate count of a node */
+} dpg_lazy_stats;
+
+int dpg_lazy_check(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x_dev, int64_t n,
+                   const uint32_t *node_dev, const uint32_t *prim_dev, const float *score_dev, int32_t score_stride,
+                   int32_t limit, dpg_expand_out *out, dpg_lazy_stats *stats);
 
 /* Allocation-free form of dpg_expand.  No counterpart in the reference (its
  * expansion runs on the host).  For callers that cannot allocate device
