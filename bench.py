@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--dropin-nodes", type=int, default=2000, help="nodes of the per-node drop-in arm")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch choices (no autotuner)")
     ap.add_argument("--arm-envs", type=int, default=40, help="training environments of the surrogate arm")
     ap.add_argument("--no-extras", action="store_true",
                     help="headline workload only: no expansion arms, no other workloads (profiling runs)")
@@ -389,8 +390,27 @@ def other_workload(args, lib, G, cfg, dev):
     with G.Context(wl.robot, device=dev) as ctx:
         ctx.upload_primitives(wl.prims)
         ctx.upload_env(wl.env)
+        tune = None
+        if not args.no_tune:
+            import torch
+            x_t = torch.from_numpy(wl.nodes).to(f"cuda:{dev}")
+            torch.cuda.synchronize()
+            tune = ctx.autotune(x_t.data_ptr(), len(wl.nodes), wl.radius, precision=wl.precision)
+            del x_t
         m = measure_device(args, lib, ctx, wl, dev, min(args.steps, 10), args.warmup)
         roof = check_roofline(lib, wl, m, dev, cfg)
+        # the same nodes with the reference loop's lazy checks (motion order,
+        # limit_branching_factor valid motions per node), against the eager
+        # expand's verdicts
+        n = m["n_pairs"]
+        eager = (m["outs"]["node"][:n].cpu().numpy().view(np.uint32),
+                 m["outs"]["prim"][:n].cpu().numpy().view(np.uint32), m["outs"]["verdict"][:n].cpu().numpy())
+        t_e, _ = timed_wall(lib, dev, min(args.steps, 10), lambda: ctx.expand_device(
+            m["x_d"].data_ptr(), len(wl.nodes), wl.radius, {k: v.data_ptr() for k, v in m["outs"].items()},
+            m["cap"], precision=wl.precision))
+        lazy = LazyArm(lib, ctx, wl, m["x_d"], dev, n, m["cap"], LIMIT_BRANCHING)
+        lz = lazy.measure(min(args.steps, 10), None, eager)
+        del lazy
         m.pop("outs")
         m.pop("x_d")
     rec = {"workload": wl.name, "robot": wl.robot.name, "dtype": "f64" if wl.precision else "f32",
@@ -400,7 +420,11 @@ def other_workload(args, lib, G, cfg, dev):
            "ms_per_step": 1e3 * m["dev_s"] / min(args.steps, 10), "check_ms": 1e3 * m["check_s"],
            "ball_ms": statistics.mean(t[0] for t in m["stage"]),
            "parity": "tests/test_parity_gpu.py::test_full_size_parity (every pair of this workload vs the oracle)",
-           "roofline": {k: roof[k] for k in ("achieved", "peak", "unit", "frac")}}
+           "roofline": {k: roof[k] for k in ("achieved", "peak", "unit", "frac")},
+           **({"tuning": tune} if tune else {}),
+           "lazy_vs_batched": {"limit_branching_factor": LIMIT_BRANCHING,
+                               "rate": "in-ball candidate pairs handled per second (wall clock)",
+                               "batched": {"value": n / t_e, "ms": 1e3 * t_e}, "batched_lazy": lz}}
     if not args.no_cpu_baseline:
         rec["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds / 2)
         rec["vs_cpu_all_cores"] = rec["value"] / rec["cpu_baseline"]["value"]
@@ -433,6 +457,14 @@ def run_ours(args, rank, world, local_rank):
     ctx.upload_env(wl.env)
     prec = wl.precision
     es_bytes = 8 if prec != 0 else 4
+
+    # ---------------- launch choices: the project's autotuner on this batch
+    tune = None
+    if not args.no_tune:
+        x_t = torch.from_numpy(wl.nodes).to(f"cuda:{dev}")
+        torch.cuda.synchronize()
+        tune = ctx.autotune(x_t.data_ptr(), N, wl.radius, precision=prec)
+        del x_t
 
     # ---------------- device-resident value
     torch.cuda.synchronize()
@@ -498,11 +530,83 @@ def run_ours(args, rank, world, local_rank):
         "stage_ms": {k: statistics.mean(t[i] for t in stage) for i, k in
                      enumerate(("ball_scan", "check", "fp64_recheck", "copies"))},
         "cpu_baseline": cpu,
+        **({"tuning": tune} if tune else {}),
         **({"expansion_arms": arms} if arms else {}),
         **({"other_workloads": others} if others else {}),
         "clocks": clk,
     }
     print(json.dumps(line, default=_np_json), flush=True)
+
+
+def timed_wall(lib, dev, steps, fn):
+    """median wall time of fn() over `steps` calls (2 warm-up calls; L2
+    flushed and the device synchronised around each)"""
+    import torch
+    for _ in range(2):
+        fn()
+    ts, r = [], None
+    for _ in range(steps):
+        lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts), r
+
+
+class LazyArm:
+    """ball-only dpg_expand + (scores) + dpg_lazy_check on the workload's
+    nodes, with device buffers for n_cand candidates"""
+
+    def __init__(self, lib, ctx, wl, x_d, dev, n_cand, cap, limit):
+        import torch
+        nx = wl.nodes.shape[1]
+        self.lib, self.ctx, self.wl, self.x_d, self.dev = lib, ctx, wl, x_d, dev
+        self.n_cand, self.cap, self.limit = n_cand, cap, limit
+        self.cand = {"node": torch.empty(cap, dtype=torch.int32, device=dev),
+                     "prim": torch.empty(cap, dtype=torch.int32, device=dev)}
+        self.cptr = {k: v.data_ptr() for k, v in self.cand.items()}
+        es_t = torch.float64 if wl.precision else torch.float32
+        self.lz = {"verdict": torch.empty(cap, dtype=torch.uint8, device=dev),
+                   "first_invalid": torch.empty(cap, dtype=torch.int16, device=dev),
+                   "end_state": torch.empty((cap, nx), dtype=es_t, device=dev),
+                   "min_gap": torch.empty(cap, dtype=torch.float32, device=dev),
+                   "flags": torch.empty(cap, dtype=torch.uint8, device=dev)}
+        self.lptr = {k: v.data_ptr() for k, v in self.lz.items()}
+
+    def run(self, score_fn=None):
+        ctx, wl, N = self.ctx, self.wl, len(self.wl.nodes)
+        ctx.expand_device(self.x_d.data_ptr(), N, wl.radius, self.cptr, self.cap, precision=wl.precision,
+                          ball_only=True)
+        sc = score_fn() if score_fn else None
+        return ctx.lazy_check_device(self.x_d.data_ptr(), N, self.n_cand, self.cptr["node"], self.cptr["prim"],
+                                     self.lptr, self.limit, score_ptr=sc.data_ptr() if sc is not None else None,
+                                     score_stride=2, precision=wl.precision)
+
+    def measure(self, steps, score_fn, eager, score_host=None):
+        """rate, exact checks, and the checks against the eager arm's
+        verdicts (eager = (node, prim, verdict) host arrays in the same
+        candidate order) and the reference loop's accepted sets"""
+        from dynoplan_gb300 import _lib
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from lazy_ref import lazy_accept
+        t, st = timed_wall(self.lib, self.dev, steps, lambda: self.run(score_fn))
+        n = self.n_cand
+        node_h, prim_h, v_eager = eager
+        v = self.lz["verdict"][:n].cpu().numpy()
+        fl = self.lz["flags"][:n].cpu().numpy()
+        same_order = (np.array_equal(self.cand["node"][:n].cpu().numpy().view(np.uint32), node_h) and
+                      np.array_equal(self.cand["prim"][:n].cpu().numpy().view(np.uint32), prim_h))
+        checked = v != _lib.DPG_UNCHECKED
+        acc = (fl & _lib.DPG_FLAG_ACCEPTED) != 0
+        score = score_host() if score_host else None
+        ref_acc, needed = lazy_accept(node_h, prim_h, v_eager == 0, score, self.limit)
+        return {"value": n / t, "ms": 1e3 * t, "exact_checks": st["n_checked"],
+                "checked_fraction": st["n_checked"] / max(n, 1), "accepted": st["n_accepted"],
+                "rounds": st["rounds"],
+                "verdicts_identical": bool(same_order and np.array_equal(v[checked], v_eager[checked])),
+                "accepted_as_reference_loop": bool(np.array_equal(acc, ref_acc) and checked[needed].all())}
 
 
 LIMIT_BRANCHING = 20   # limit_branching_factor default (include/dynoplan/dbastar/options.hpp)
@@ -536,8 +640,6 @@ def run_arms(args, lib, G, ctx, wl, x_d, dev):
     from dynoplan_gb300 import _lib
     from dynoplan_gb300 import surrogate as SG
     from dynoplan_gb300 import workloads as W
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from lazy_ref import lazy_accept
     N, nx = wl.nodes.shape
     limit = LIMIT_BRANCHING
     steps = max(3, min(args.steps, 10))
@@ -563,59 +665,17 @@ def run_arms(args, lib, G, ctx, wl, x_d, dev):
     eag = device_outputs(torch, cap, nx, 0, dev)
     eptr = {k: v.data_ptr() for k, v in eag.items()}
 
-    def timed(fn):
-        for _ in range(2):
-            fn()
-        ts = []
-        for _ in range(steps):
-            lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            r = fn()
-            torch.cuda.synchronize()
-            ts.append(time.perf_counter() - t0)
-        return statistics.median(ts), r
-
-    t_b, _ = timed(lambda: ctx.expand_device(x_d.data_ptr(), N, wl.radius, eptr, cap, precision=0))
+    t_b, _ = timed_wall(lib, dev, steps, lambda: ctx.expand_device(x_d.data_ptr(), N, wl.radius, eptr, cap,
+                                                                     precision=0))
     out["batched"] = {"value": n_cand / t_b, "ms": 1e3 * t_b, "checked_pairs": n_cand}
     v_eager = eag["verdict"][:n_cand].cpu().numpy()
     node_h = eag["node"][:n_cand].cpu().numpy().view(np.uint32)
     prim_h = eag["prim"][:n_cand].cpu().numpy().view(np.uint32)
 
     # ---- lazy arms: candidates, (scores), lazy check
-    cand = {"node": torch.empty(cap, dtype=torch.int32, device=dev),
-            "prim": torch.empty(cap, dtype=torch.int32, device=dev)}
-    cptr = {k: v.data_ptr() for k, v in cand.items()}
-    lz = {"verdict": torch.empty(cap, dtype=torch.uint8, device=dev),
-          "first_invalid": torch.empty(cap, dtype=torch.int16, device=dev),
-          "end_state": torch.empty((cap, nx), dtype=torch.float32, device=dev),
-          "min_gap": torch.empty(cap, dtype=torch.float32, device=dev),
-          "flags": torch.empty(cap, dtype=torch.uint8, device=dev)}
-    lptr = {k: v.data_ptr() for k, v in lz.items()}
+    lazy = LazyArm(lib, ctx, wl, x_d, dev, n_cand, cap, limit)
 
-    def lazy_arm(score_fn):
-        def fn():
-            ctx.expand_device(x_d.data_ptr(), N, wl.radius, cptr, cap, precision=0, ball_only=True)
-            sc = score_fn() if score_fn else None
-            return ctx.lazy_check_device(x_d.data_ptr(), N, n_cand, cptr["node"], cptr["prim"], lptr, limit,
-                                         score_ptr=sc.data_ptr() if sc is not None else None, score_stride=2)
-        return fn
-
-    def verify(st, score):
-        v = lz["verdict"][:n_cand].cpu().numpy()
-        fl = lz["flags"][:n_cand].cpu().numpy()
-        same_order = (np.array_equal(cand["node"][:n_cand].cpu().numpy().view(np.uint32), node_h) and
-                      np.array_equal(cand["prim"][:n_cand].cpu().numpy().view(np.uint32), prim_h))
-        checked = v != _lib.DPG_UNCHECKED
-        acc = (fl & _lib.DPG_FLAG_ACCEPTED) != 0
-        ref_acc, needed = lazy_accept(node_h, prim_h, v_eager == 0, score, limit)
-        return {"exact_checks": st["n_checked"], "checked_fraction": st["n_checked"] / n_cand,
-                "accepted": st["n_accepted"], "rounds": st["rounds"],
-                "verdicts_identical": bool(same_order and np.array_equal(v[checked], v_eager[checked])),
-                "accepted_as_reference_loop": bool(np.array_equal(acc, ref_acc) and checked[needed].all())}
-
-    t_l, st = timed(lazy_arm(None))
-    out["batched_lazy"] = {"value": n_cand / t_l, "ms": 1e3 * t_l, **verify(st, None)}
+    out["batched_lazy"] = lazy.measure(steps, None, (node_h, prim_h, v_eager))
 
     # surrogate: trained first (outside the timing) on exact labels of other
     # environments of the workload's kind; the bench environment is held out
@@ -628,13 +688,12 @@ def run_arms(args, lib, G, ctx, wl, x_d, dev):
 
     def score_fn():
         feat = SG.node_features(ctx, x_d)
-        return model.forward(feat, cand["node"][:n_cand], cand["prim"][:n_cand], logits[:n_cand])
+        return model.forward(feat, lazy.cand["node"][:n_cand], lazy.cand["prim"][:n_cand], logits[:n_cand])
 
-    t_s, st = timed(lazy_arm(score_fn))
+    out["batched_lazy_surrogate"] = lazy.measure(steps, score_fn, (node_h, prim_h, v_eager),
+                                                 score_host=lambda: logits[:n_cand, 0].cpu().numpy())
+    out["batched_lazy_surrogate"]["forward_ms"] = model.timing()[0]
     score_h = logits[:n_cand, 0].cpu().numpy()
-    mlp_ms = model.timing()[0]
-    out["batched_lazy_surrogate"] = {"value": n_cand / t_s, "ms": 1e3 * t_s, "forward_ms": mlp_ms,
-                                     **verify(st, score_h)}
     y = v_eager != 0
     pred = score_h > 0
     tp = int((pred & y).sum())

@@ -23,6 +23,8 @@ DPG_ERR_CAPACITY = -6
 DPG_ERR_STATE = -7
 DPG_ERR_NODEVICE = -8
 DPG_UNCHECKED = 255
+DPG_CHECK_LOCKSTEP = 0
+DPG_CHECK_SLOTS = 1
 DPG_FLAG_ACCEPTED = 2
 
 DPG_FP32 = 0
@@ -46,6 +48,17 @@ class ExpandOpts(C.Structure):
         ("out_on_device", C.c_int32), ("mode", C.c_int32),
         ("contact_band", C.c_double), ("ball_band", C.c_double),
     ]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("check_variant", C.c_int32), ("check_blocks_per_sm", C.c_int32),
+                ("grid_min_nodes", C.c_int32), ("pipe_launches", C.c_int32)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("chosen", Tuning), ("initial", Tuning), ("ms_chosen", C.c_double), ("ms_initial", C.c_double),
+                ("seconds", C.c_double), ("candidates", C.c_int32), ("from_cache", C.c_int32),
+                ("key", C.c_char * 160)]
 
 
 class LazyStats(C.Structure):
@@ -84,7 +97,13 @@ SIGNATURES = [
     ("dpg_lazy_check", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p, C.c_int64,
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(ExpandOut),
                                  C.POINTER(LazyStats)]),
+    ("dpg_get_tuning", C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    ("dpg_set_tuning", C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     ("dpg_sync", C.c_int, [C.c_void_p]),
+    # include/dpg_tune.h
+    ("dpg_autotune", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p, C.c_int32, C.c_char_p,
+                               C.POINTER(TuneReport)]),
+    ("dpg_tune_key", C.c_int, [C.c_void_p, C.c_int64, C.c_char_p, C.c_int32]),
     ("dpg_set_abort", C.c_int, [C.c_void_p, C.c_int32]),
     ("dpg_host_alloc", C.c_void_p, [C.c_size_t]),
     ("dpg_host_free", None, [C.c_void_p]),

@@ -17,7 +17,7 @@ LIB = os.path.join(_HERE, "libdpg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
-SOURCES = ["dpg.cu", "bench_util.cu", "mlp.cu", "search.cu", "prim_io.cu", "roadmap.cu", "tdb.cu", "lazy.cu"]
+SOURCES = ["dpg.cu", "bench_util.cu", "mlp.cu", "search.cu", "prim_io.cu", "roadmap.cu", "tdb.cu", "lazy.cu", "tune.cu"]
 
 
 def nvcc() -> str:

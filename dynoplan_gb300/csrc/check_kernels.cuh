@@ -55,6 +55,8 @@ struct CheckArgs {
   // when set, the pair's node id is written back through it (processing
   // order -> caller's numbering) once the pair is checked
   const uint32_t *perm;
+  // slot variant: byte offset of the per-warp scratch in dynamic shared memory
+  int slot_offset;
 };
 
 template <class Real> __device__ __forceinline__ const Pose<Real> *pose_table(const PrimView &pv);
@@ -448,6 +450,357 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   }
 }
 
+// ------------------------------------------------- slot-parallel variant --
+//
+// The lockstep walk above makes every state cost the largest candidate count
+// of any lane: lanes with fewer candidates (most have none) wait.  This
+// variant keeps the walk over chunks of R::CHUNK states but runs each
+// chunk's narrow phase as a list of (lane, candidate obstacle) slots spread
+// over the warp's 32 lanes; a slot tests its obstacle against every state of
+// the chunk (all parts) and stops at its first contact.  Per lane and state,
+// the contacts, the FP64 decisions and the minimum axis-aligned gap are merged
+// in shared memory; each lane then folds the states up to its first contact,
+// which gives exactly the per-state results of the sequential walk (every
+// candidate is tested at every state up to the first contact).  FP32 tests
+// with FP64 decisions in the band; the bounds tests stay per lane.
+
+template <int CH, int PARTS> struct SlotScratch {
+  Pose<float> pose[CH * PARTS];  // the chunk's pose rows, [j * PARTS + q]
+  unsigned mg[32][CH];           // per lane and state: min axis-aligned gap (order-preserving bits)
+  unsigned hit[32];              // per lane: bit j = contact at state k0 + j
+  unsigned rc[32];               // per lane: bit j = a test at k0 + j was decided in FP64
+};
+
+__device__ __forceinline__ unsigned ord_gap(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float unord_gap(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+template <int KIND>
+constexpr size_t slot_scratch_bytes() {
+  return sizeof(SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS>);
+}
+
+template <int KIND, int NW, bool ES64>
+__device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
+                                SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS> &S, int p, int64_t pair,
+                                uint32_t node, bool active) {
+  using R = Robot<KIND>;
+  constexpr int D = R::POSD, V = R::VELOFF, CH = R::CHUNK, PARTS = R::PARTS;
+  static_assert(NW > 0, "the slot variant needs the candidate bitmasks");
+  const int lane = threadIdx.x & 31;
+  const PrimView &pv = A.pv;
+  const RobotParams &rp = A.rp;
+  const int L = pv.len[p];
+  const int64_t s0 = pv.soff[p];
+  const Pose<float> *pose = pv.pose32;
+  const float band = A.band32, dt = A.dt32;
+  const double *x64 = A.nv.x64 + (int64_t)(active ? node : 0) * R::NX;
+  const int n_obs = A.ev.n_obs;
+
+  float off[D + V];
+#pragma unroll
+  for (int i = 0; i < D; i++) off[i] = active ? node_off<float>(A.nv, node, i, R::NX, i) : 0.f;
+#pragma unroll
+  for (int i = 0; i < V; i++) off[D + i] = active ? node_off<float>(A.nv, node, D + i, R::NX, R::vel_comp(i)) : 0.f;
+
+  // bounds pre-check on the swept box of the positions (as check_one)
+  bool need_bounds = true;
+  if (active) {
+    const float *bx32 = pv.pbox32 + (int64_t)p * 2 * D;
+    const float tmax = float(L - 1) * dt;
+    bool inside = true;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      float lo = bx32[i] + off[i], hi = bx32[D + i] + off[i];
+      if (V) {
+        const float sv = tmax * off[D + i];
+        lo += fminf(sv, 0.f);
+        hi += fmaxf(sv, 0.f);
+      }
+      inside = inside && lo > A.lo32[i] + band + 1e-3f && hi < A.hi32[i] - band - 1e-3f;
+    }
+    need_bounds = !inside;
+  }
+
+  // level-1 culling against the whole transformed primitive
+  uint32_t l1[NW] = {};
+  const float M = A.cull_margin;
+  if (active) {
+    const float *tb = pv.tbox32 + (int64_t)p * 2 * D;
+    const float tmax = float(L - 1) * dt;
+    float cen[D], hf[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      cen[i] = tb[i] + off[i];
+      hf[i] = tb[D + i];
+      if (V) {
+        const float sv = tmax * off[D + i];
+        cen[i] += 0.5f * sv;
+        hf[i] += 0.5f * fabsf(sv);
+      }
+    }
+#pragma unroll
+    for (int w = 0; w < NW; w++) {
+      uint32_t bits = 0u;
+      const int o0 = 32 * w, o1 = min(n_obs, o0 + 32);
+      for (int o = o0; o < o1; o++)
+        if (near_box<D, float>(cen, hf, obs_sm, o, M)) bits |= 1u << (o - o0);
+      l1[w] = bits;
+    }
+  }
+
+  bool done = !active, collided = false, rechecked = false;
+  int first_oob = L, first_col = L;
+  float mg = INFINITY;
+  const float hl = A.half_len32, hw = A.half_wid32, rad = A.radius32;
+
+  for (int k0 = 0; k0 < L; k0 += CH) {
+    if (!__any_sync(kFull, !done)) break;
+    const int kend = min(L, k0 + CH);
+    // the chunk's box: level-2 culling and whether its states need bounds tests
+    uint32_t cm[NW];
+#pragma unroll
+    for (int w = 0; w < NW; w++) cm[w] = 0u;
+    bool nb = false;
+    if (!done) {
+      const float *cb = pv.cbox32 + (pv.coff[p] + k0 / CH) * 2 * D;
+      const float t0 = float(k0) * dt, t1 = float(kend - 1) * dt;
+      float cen[D], hf[D];
+#pragma unroll
+      for (int i = 0; i < D; i++) {
+        cen[i] = cb[i] + off[i];
+        hf[i] = cb[D + i];
+        if (V) {
+          const float v = off[D + i];
+          cen[i] += 0.5f * (t0 + t1) * v;
+          hf[i] += 0.5f * (t1 - t0) * fabsf(v);
+        }
+      }
+      if (!collided) {
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+          uint32_t m = l1[w], c = 0;
+          while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            if (near_box<D, float>(cen, hf, obs_sm, 32 * w + b, M)) c |= 1u << b;
+          }
+          cm[w] = c;
+        }
+      }
+      if (need_bounds) {
+        bool in = true;
+#pragma unroll
+        for (int i = 0; i < D; i++)
+          in = in && cen[i] - hf[i] > A.lo32[i] + band + 1e-3f && cen[i] + hf[i] < A.hi32[i] - band - 1e-3f;
+        nb = !in;
+      }
+    }
+    // bounds tests of the chunk's states, per lane, up to the first state out
+    int j_oob = CH;
+    if (nb) {
+      for (int k = k0; k < kend; k++) {
+        const Pose<float> ps = pose[s0 + k];  // part 0 = the state position
+        const float t = float(k) * dt;
+        const float pv3[3] = {ps.cx + off[0] + (V ? t * off[D] : 0.f), ps.cy + off[1] + (V ? t * off[D + 1] : 0.f),
+                              D == 3 ? ps.c + off[2] + (V ? t * off[D + 2] : 0.f) : 0.f};
+        int bt = 0;
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+          const float v = pv3[i], lo = A.lo32[i], hi = A.hi32[i];
+          int r = (v < lo - band || v > hi + band) ? 1 : ((v <= lo + band || v >= hi - band) ? 2 : 0);
+          if (r == 2) {  // decide in FP64
+            const double v64 = pos64<KIND>(A, s0 + k, k, x64, i);
+            r = (v64 >= A.ev.lo[i] && v64 <= A.ev.hi[i]) ? 0 : 1;
+            rechecked = true;
+          }
+          bt |= r;
+        }
+        if (bt) {
+          j_oob = k - k0;
+          break;
+        }
+      }
+    }
+    // the narrow phase as (lane, candidate) slots
+    const int nst = (!done && !collided) ? min(kend - k0, j_oob) : 0;
+    int nc = 0;
+    if (nst > 0) {
+#pragma unroll
+      for (int w = 0; w < NW; w++) nc += __popc(cm[w]);
+    }
+    int pre = nc;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(kFull, pre, d);
+      if (lane >= d) pre += v;
+    }
+    const int T = __shfl_sync(kFull, pre, 31);
+    pre -= nc;  // exclusive prefix
+    if (T > 0) {
+      if (lane < CH * PARTS) {
+        const int j = lane / PARTS, q = lane % PARTS;
+        if (k0 + j < L) S.pose[lane] = pose[(int64_t)q * pv.S + s0 + k0 + j];
+      }
+#pragma unroll
+      for (int j = 0; j < CH; j++) S.mg[lane][j] = ord_gap(INFINITY);
+      S.hit[lane] = 0u;
+      S.rc[lane] = 0u;
+      __syncwarp();
+      for (int base = 0; base < T; base += 32) {
+        const int t = base + lane;
+        int owner = 0;  // the last lane whose exclusive prefix is <= t
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+          const int cand = owner + step;
+          const int pv_ = __shfl_sync(kFull, pre, cand & 31);
+          if (cand < 32 && pv_ <= t) owner = cand;
+        }
+        const int opre = __shfl_sync(kFull, pre, owner);
+        const int onst = __shfl_sync(kFull, nst, owner);
+        const uint32_t onode = __shfl_sync(kFull, node, owner);
+        uint32_t ocm[NW];
+#pragma unroll
+        for (int w = 0; w < NW; w++) ocm[w] = __shfl_sync(kFull, cm[w], owner);
+        float osh[D + V];
+#pragma unroll
+        for (int i = 0; i < D + V; i++) osh[i] = __shfl_sync(kFull, off[i], owner);
+        if (t < T) {
+          int cidx = t - opre, o = -1;
+#pragma unroll
+          for (int w = 0; w < NW; w++) {
+            const int c = __popc(ocm[w]);
+            if (o < 0) {
+              if (cidx < c) o = 32 * w + (int)__fns(ocm[w], 0u, cidx + 1);
+              else cidx -= c;
+            }
+          }
+          if (o >= 0 && o < n_obs) {
+            const double *ox64 = A.nv.x64 + (int64_t)onode * R::NX;
+            for (int j = 0; j < onst; j++) {
+              const int k = k0 + j;
+              const float tk = float(k) * dt;
+              float sx = osh[0], sy = osh[1], sz = 0.f;
+              if (V) {
+                sx += tk * osh[D + 0];
+                sy += tk * osh[D + 1];
+              }
+              if (D == 3) {
+                sz = osh[2];
+                if (V) sz += tk * osh[D + 2];
+              }
+              float g = INFINITY;
+              bool hit = false;
+#pragma unroll
+              for (int q = 0; q < PARTS; q++) {
+                const Pose<float> ps = S.pose[j * PARTS + q];
+                int r;
+                if constexpr (R::SPHERE) {
+                  const Obs3<float> ob = ((const Obs3<float> *)obs_sm)[o];
+                  r = sphere_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c + sz, ob, rad, band, g);
+                } else {
+                  const Obs2<float> ob = ((const Obs2<float> *)obs_sm)[o];
+                  const float ac = fabsf(ps.c), as = fabsf(ps.s);
+                  r = planar_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c, ps.s, hl * ac + hw * as,
+                                               hl * as + hw * ac, ob, hl, hw, band, g);
+                }
+                if (r == 2) {  // decide in FP64
+                  r = gap64<KIND>(A, s0, k, q, ox64, o) <= 0.0 ? 1 : 0;
+                  atomicOr(&S.rc[owner], 1u << j);
+                }
+                hit |= r == 1;
+              }
+              atomicMin(&S.mg[owner][j], ord_gap(g));
+              if (hit) {
+                atomicOr(&S.hit[owner], 1u << j);
+                break;  // later states of this candidate lie past the lane's first contact
+              }
+            }
+          }
+        }
+      }
+      __syncwarp();
+      if (nst > 0) {
+        const unsigned h = S.hit[lane];
+        const int last = h ? __ffs(h) - 1 : nst - 1;
+        for (int j = 0; j <= last; j++) mg = fminf(mg, unord_gap(S.mg[lane][j]));
+        if (S.rc[lane] & (last >= 31 ? 0xffffffffu : ((2u << last) - 1u))) rechecked = true;
+        if (h) {
+          collided = true;
+          first_col = k0 + last;
+        }
+      }
+      __syncwarp();  // the next chunk reuses the scratch
+    }
+    if (!done) {
+      if (j_oob < CH) {
+        first_oob = k0 + j_oob;
+        done = true;
+      } else if (collided && !need_bounds) {
+        done = true;
+      }
+    }
+  }
+
+  const unsigned rmask = __ballot_sync(kFull, active && rechecked);
+  if (lane == 0 && rmask) atomicAdd(&A.ctr->n_recheck, (unsigned long long)__popc(rmask));
+  if (!active) return;
+  const PairView &o = A.out;
+  if (A.perm) o.node[pair] = A.perm[node];
+  uint8_t verdict;
+  int fi;
+  if (first_oob < L) { verdict = DPG_OUT_OF_BOUNDS; fi = first_oob; }
+  else if (collided) { verdict = DPG_COLLISION; fi = first_col; }
+  else { verdict = DPG_VALID; fi = L; }
+  const int er = first_oob < L ? first_oob : L - 1;  // end-state row
+  const int64_t row_out = o.out_index ? (int64_t)o.out_index[pair] : pair;
+  if (o.verdict) o.verdict[row_out] = verdict;
+  if (o.first_invalid) o.first_invalid[row_out] = (int16_t)fi;
+  if (o.min_gap)
+    o.min_gap[row_out] = verdict == DPG_OUT_OF_BOUNDS ? __int_as_float(0x7fc00000)
+                                                   : (mg <= kGapCap ? mg : __int_as_float(0x7f800000));
+  if (o.flags) o.flags[row_out] = rechecked ? DPG_FLAG_CONTACT_RECHECK : 0;
+  if (o.end_state) {
+    if constexpr (ES64) {
+      double *es = (double *)o.end_state + row_out * R::NX;
+      const double t = double(er) * rp.dt;
+      const double *xs = pv.st64 + (s0 + er) * R::NX;
+#pragma unroll
+      for (int c = 0; c < R::NX; c++) {
+        double v = xs[c];
+        if (c < D) {
+          v += x64[c];
+          if (V) v += t * x64[R::vel_comp(c)];
+        }
+#pragma unroll
+        for (int i = 0; i < V; i++)
+          if (c == R::vel_comp(i)) v += x64[R::vel_comp(i)];
+        es[c] = v;
+      }
+    } else {
+      float *es = (float *)o.end_state + row_out * R::NX;
+      const float t = float(er) * dt;
+      const int64_t row = s0 + er;
+#pragma unroll
+      for (int c = 0; c < R::NX; c++) {
+        float v = pv.st32[row * R::NX + c];
+        if (c < D) {
+          v += off[c];
+          if (V) v += t * off[D + c];
+        }
+#pragma unroll
+        for (int i = 0; i < V; i++)
+          if (c == R::vel_comp(i)) v += off[D + i];
+        es[c] = v;
+      }
+    }
+  }
+}
+
 template <class Real, int KIND>
 __device__ void load_obstacles(const EnvView &ev, void *sm) {
   using R = Robot<KIND>;
@@ -464,7 +817,9 @@ __device__ void load_obstacles(const EnvView &ev, void *sm) {
 }
 
 // Persistent warps over (primitive, 32 nodes) work items.
-template <int KIND, class Real, bool BAND, int NW, bool ES64 = false>
+// SLOTS: the slot-parallel narrow phase (FP32 tests with the band, NW > 0);
+// its per-warp scratch follows the obstacles at A.slot_offset.
+template <int KIND, class Real, bool BAND, int NW, bool ES64 = false, bool SLOTS = false>
 __global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) check_pairs(CheckArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   load_obstacles<Real, KIND>(A.ev, smem);
@@ -500,7 +855,13 @@ __global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) chec
     const unsigned long long pair = first + lane;
     const bool active = pair < end;
     const uint32_t node = active ? A.out.node[pair] : 0u;
-    check_one<KIND, Real, BAND, NW, true, ES64>(A, smem, p, (int64_t)pair, node, active);
+    if constexpr (SLOTS) {
+      using Scratch = SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS>;
+      Scratch *scr = reinterpret_cast<Scratch *>(smem + A.slot_offset) + (threadIdx.x >> 5);
+      check_one_slots<KIND, NW, ES64>(A, smem, *scr, p, (int64_t)pair, node, active);
+    } else {
+      check_one<KIND, Real, BAND, NW, true, ES64>(A, smem, p, (int64_t)pair, node, active);
+    }
   }
 }
 

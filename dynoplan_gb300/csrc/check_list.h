@@ -19,6 +19,13 @@ EnvView ctx_env_view(const dpg_ctx *c);
 // prepared) and outputs; prec is DPG_FP32, DPG_FP64 or DPG_FP64_STRICT.
 CheckArgs ctx_check_args(dpg_ctx *c, int prec, double contact_band, const NodeView &nv, const PairView &out);
 
+// Processing order of N nodes (x_dev: N x nx, caller's order) on st:
+// *perm[pos] = the caller's index of the node at position pos -- Z-order
+// cells over the environment, ascending index within a cell, as dpg_expand
+// processes a batch.  Batches under kReorderMin nodes keep the caller's
+// order (*perm = nullptr).  Uses the context's ordering buffers.
+int ctx_spatial_order(dpg_ctx *c, const double *x_dev, int64_t N, cudaStream_t st, const uint32_t **perm);
+
 // node keys / offsets of nv (prep_nodes) on st
 void ctx_prep_nodes(dpg_ctx *c, const NodeView &nv, cudaStream_t st);
 
@@ -32,5 +39,13 @@ void ctx_prep_nodes(dpg_ctx *c, const NodeView &nv, cudaStream_t st);
 // check kernel when `timed`.
 int ctx_check_list(dpg_ctx *c, int prec, CheckArgs ca, int64_t n, const uint32_t *node_d, const uint32_t *prim_d,
                    const uint32_t *dest_d, cudaStream_t st, bool timed);
+
+// Exact check of a list already grouped by primitive: the segments of the
+// primitives in length order (pv.order) start at c->ord_pbase and their
+// work items at c->ord_ibase (scan_totals has written them and the
+// counters' n_items); list_node[i] is the node, list_dest[i] the output row
+// of list entry i.  Does not wait.
+int ctx_check_grouped(dpg_ctx *c, int prec, CheckArgs ca, const uint32_t *list_node, const uint32_t *list_dest,
+                      cudaStream_t st);
 
 }  // namespace dpg

@@ -125,21 +125,28 @@ static void launch_check(dpg_ctx *c, const CheckArgs &ca, int prec, cudaStream_t
   const int nw = c->n_obs <= 32 ? 1 : c->n_obs <= 64 ? 2 : c->n_obs <= 96 ? 3 : c->n_obs <= kMaxCullObs ? 4 : 0;
   const size_t ob = fp64 ? (R::SPHERE ? sizeof(Obs3<double>) : sizeof(Obs2<double>))
                          : (R::SPHERE ? sizeof(Obs3<float>) : sizeof(Obs2<float>));
-  const size_t sm = ob * std::max(c->n_obs, 1);
+  const size_t sm_obs = (ob * std::max(c->n_obs, 1) + 15) / 16 * 16;
+  // the slot-parallel narrow phase for FP32 tests with culling
+  const bool slots = !fp64 && nw > 0 && c->tune.check_variant == DPG_CHECK_SLOTS;
+  const size_t sm = sm_obs + (slots ? slot_scratch_bytes<KIND>() * (kCheckThreads / 32) : 0);
+  CheckArgs a = ca;
+  a.slot_offset = (int)sm_obs;
   auto go = [&](auto kern) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
-    kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(ca);
+    if (c->tune.check_blocks_per_sm > 0) per_sm = std::min(per_sm, c->tune.check_blocks_per_sm);
+    kern<<<c->sm_count * std::max(per_sm, 1), kCheckThreads, sm, st>>>(a);
   };
   auto by_words = [&](auto real, auto band, auto es64) {
     using Real = decltype(real);
     constexpr bool BAND = decltype(band)::value, ES64 = decltype(es64)::value;
+    constexpr bool F32 = sizeof(Real) == 4;
     switch (nw) {
-      case 1: go(check_pairs<KIND, Real, BAND, 1, ES64>); break;
-      case 2: go(check_pairs<KIND, Real, BAND, 2, ES64>); break;
-      case 3: go(check_pairs<KIND, Real, BAND, 3, ES64>); break;
-      case 4: go(check_pairs<KIND, Real, BAND, 4, ES64>); break;
+      case 1: slots ? go(check_pairs<KIND, Real, BAND, 1, ES64, F32>) : go(check_pairs<KIND, Real, BAND, 1, ES64>); break;
+      case 2: slots ? go(check_pairs<KIND, Real, BAND, 2, ES64, F32>) : go(check_pairs<KIND, Real, BAND, 2, ES64>); break;
+      case 3: slots ? go(check_pairs<KIND, Real, BAND, 3, ES64, F32>) : go(check_pairs<KIND, Real, BAND, 3, ES64>); break;
+      case 4: slots ? go(check_pairs<KIND, Real, BAND, 4, ES64, F32>) : go(check_pairs<KIND, Real, BAND, 4, ES64>); break;
       default: go(check_pairs<KIND, Real, BAND, 0, ES64>); break;
     }
   };
@@ -162,13 +169,12 @@ static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
 // Ball scan of the nv.N nodes against the pv.P primitives: bitmask words
 // (P x Wpad, primitive-major), per-tile counts cnt[B][P] turned into prefixes,
 // totals tot[P].
-// Batches of at least kGridMin nodes of a robot with a key grid test only the
+// Batches of at least tune.grid_min_nodes nodes of a robot with a key grid test only the
 // primitives of the cells near their key; smaller batches test every
 // primitive (split over the primitives too, to fill the GPU).  Both give the
 // same mask and counts.
-constexpr int64_t kGridMin = 2048;
-constexpr int kPipe = 8;  // check launches of an expand whose results go to host buffers
-static_assert(kPipe <= kMaxSub, "one work-queue counter per check launch");
+// (an expand whose results go to host buffers runs tune.pipe_launches <=
+// kMaxSub check launches, one work-queue counter each)
 template <int KIND>
 static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv, double radius, double ball_band,
                         int64_t Wpad, int64_t B, int64_t W, uint32_t *mask, uint32_t *cnt, uint32_t *tot,
@@ -179,7 +185,7 @@ static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv
   const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
   bool done = false;
   if constexpr (R::KEYD <= 2) {
-    if (c->kg.n0 > 0 && nv.N >= kGridMin) {
+    if (c->kg.n0 > 0 && nv.N >= c->tune.grid_min_nodes) {
       // half-width of the cell range along a key component: radius plus band
       // over its weight, widened; -1 = every cell
       auto half = [&](double wk, bool periodic) -> float {
@@ -315,7 +321,7 @@ void dpg_destroy(dpg_ctx *c) {
                     &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill,
                     &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_rank, &c->ord_tiles, &c->x64s,
                     &c->kg_start, &c->kg_tab, &c->lz_off, &c->lz_cnt, &c->lz_cur, &c->lz_next, &c->lz_valid,
-                    &c->lz_rank, &c->lz_lnode, &c->lz_lprim, &c->lz_ldest, &c->lz_ctr};
+                    &c->lz_rank, &c->lz_lnode, &c->lz_ldest, &c->lz_ctr, &c->lz_table};
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
@@ -613,6 +619,22 @@ int dpg_last_timings(const dpg_ctx *c, double *t, int32_t n) {
   return k;
 }
 
+int dpg_get_tuning(const dpg_ctx *c, dpg_tuning *t) {
+  if (!c || !t) return DPG_ERR_ARG;
+  *t = c->tune;
+  return DPG_OK;
+}
+
+int dpg_set_tuning(dpg_ctx *c, const dpg_tuning *t) {
+  if (!c || !t) return DPG_ERR_ARG;
+  if ((t->check_variant != DPG_CHECK_LOCKSTEP && t->check_variant != DPG_CHECK_SLOTS) ||
+      t->check_blocks_per_sm < 0 || t->check_blocks_per_sm > 32 || t->grid_min_nodes < 0 ||
+      t->pipe_launches < 1 || t->pipe_launches > kMaxSub)
+    return fail(c, DPG_ERR_ARG, "set_tuning: value out of range");
+  c->tune = *t;
+  return DPG_OK;
+}
+
 int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double *x, dpg_expand_out *out) {
   if (!c || !opts || !out) return DPG_ERR_ARG;
   if (!c->have_prims || !c->have_env) return fail(c, DPG_ERR_STATE, "expand: upload primitives and env first");
@@ -685,7 +707,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   }
 
   // host-buffer outputs of a checked batch in spatial order: the check runs as
-  // kPipe launches over item ranges and each range's results are copied out
+  // tune.pipe_launches launches over item ranges and each range's results are copied out
   // while the next range is checked
   const bool pipelined = !dev_out && !(opts->mode & DPG_MODE_BALL_ONLY) && reorder && cap > 0;
   if (pipelined) {
@@ -825,7 +847,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       // work-queue counters), so the next range's blocks take the SMs that
       // the previous range's last items leave idle
       ca.perm = reorder ? P_<uint32_t>(c->ord_perm) : nullptr;
-      ca.nsub = pipelined ? kPipe : 1;
+      ca.nsub = pipelined ? c->tune.pipe_launches : 1;
       for (int j = 0; j < ca.nsub; j++) {
         ca.sub = j;
         cudaStream_t s = pipelined && (j & 1) ? c->xstream : st;
@@ -862,8 +884,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
           {out->node, c->p_node.p, 4}, {out->prim, c->p_prim.p, 4}, {out->verdict, c->p_verdict.p, 1},
           {out->first_invalid, c->p_fi.p, 2}, {out->end_state, c->p_end.p, es_bytes * nx},
           {out->min_gap, c->p_gap.p, 4}, {out->flags, c->p_flags.p, 1}};
-      for (int j = 0; j < kPipe; j++) {
-        const int64_t a = pair_at(h0.n_items * j / kPipe), e = pair_at(h0.n_items * (j + 1) / kPipe);
+      const int np = c->tune.pipe_launches;
+      for (int j = 0; j < np; j++) {
+        const int64_t a = pair_at(h0.n_items * j / np), e = pair_at(h0.n_items * (j + 1) / np);
         CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev_sub[j], 0));
         if (e > a)
           for (const auto &f : cp)
@@ -1195,6 +1218,34 @@ CheckArgs ctx_check_args(dpg_ctx *c, int prec, double contact_band, const NodeVi
   return ca;
 }
 
+int ctx_spatial_order(dpg_ctx *c, const double *x_dev, int64_t N, cudaStream_t st, const uint32_t **perm) {
+  *perm = nullptr;
+  if (N < kReorderMin) return DPG_OK;
+  const int64_t tile = order_tile(N), ntile = (N + tile - 1) / tile;
+  int rc;
+  if ((rc = ensure(c, c->ord_cell, sizeof(uint32_t) * N)) || (rc = ensure(c, c->ord_perm, sizeof(uint32_t) * N)) ||
+      (rc = ensure(c, c->ord_cnt, sizeof(uint32_t) * kOrderCells)) ||
+      (rc = ensure(c, c->ord_start, sizeof(uint32_t) * kOrderCells)) ||
+      (rc = ensure(c, c->ord_rank, sizeof(uint32_t) * N)) ||
+      (rc = ensure(c, c->ord_tiles, sizeof(uint32_t) * kOrderCells * (size_t)ntile)))
+    return rc;
+  const EnvView ev = ctx_env_view(c);
+  with_kind(c->robot.kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    node_tiles<KIND><<<(unsigned)ntile, 256, 0, st>>>(x_dev, N, ev, tile, P_<uint32_t>(c->ord_cell),
+                                                       P_<uint32_t>(c->ord_rank), P_<uint32_t>(c->ord_tiles));
+    nn_prefix<<<kOrderCells / 32, 256, 0, st>>>(kOrderCells, (int)ntile, P_<uint32_t>(c->ord_tiles),
+                                                P_<uint32_t>(c->ord_cnt));
+    cell_scan<<<1, 1024, 0, st>>>(kOrderCells, P_<uint32_t>(c->ord_cnt), P_<uint32_t>(c->ord_start));
+    cell_scatter<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, tile, P_<uint32_t>(c->ord_cell),
+                                                             P_<uint32_t>(c->ord_rank), P_<uint32_t>(c->ord_tiles),
+                                                             P_<uint32_t>(c->ord_start), P_<uint32_t>(c->ord_perm));
+  });
+  CUDA_TRY(c, cudaGetLastError());
+  *perm = P_<uint32_t>(c->ord_perm);
+  return DPG_OK;
+}
+
 void ctx_prep_nodes(dpg_ctx *c, const NodeView &nv, cudaStream_t st) {
   if (nv.N <= 0) return;
   with_kind(c->robot.kind, [&](auto K) {
@@ -1243,6 +1294,28 @@ int ctx_check_list(dpg_ctx *c, int prec, CheckArgs ca, int64_t n, const uint32_t
     if (timed) cudaEventRecord(c->ev[2], st);
     launch_check<KIND>(c, ca, prec, st);
     if (timed) cudaEventRecord(c->ev[3], st);
+    launch_err = cudaGetLastError();
+  });
+  if (launch_err != cudaSuccess)
+    return fail(c, DPG_ERR_CUDA, std::string("check launch: ") + cudaGetErrorString(launch_err));
+  return DPG_OK;
+}
+
+int ctx_check_grouped(dpg_ctx *c, int prec, CheckArgs ca, const uint32_t *list_node, const uint32_t *list_dest,
+                      cudaStream_t st) {
+  ca.ord_pbase = P_<unsigned long long>(c->ord_pbase);
+  ca.ord_ibase = P_<unsigned long long>(c->ord_ibase);
+  ca.ctr = c->d_ctr;
+  ca.out.node = const_cast<uint32_t *>(list_node);
+  ca.out.prim = nullptr;
+  ca.out.out_index = list_dest;
+  ca.perm = nullptr;
+  ca.sub = 0;
+  ca.nsub = 1;
+  cudaError_t launch_err = cudaSuccess;
+  with_kind(c->robot.kind, [&](auto K) {
+    constexpr int KIND = decltype(K)::value;
+    launch_check<KIND>(c, ca, prec, st);
     launch_err = cudaGetLastError();
   });
   if (launch_err != cudaSuccess)

@@ -13,8 +13,13 @@
 //                                  in shared memory, one block per node
 //   rounds of
 //     lz_select                    every node short of `limit` valid motions
-//                                  lists its next ceil((limit - valid) * f)
+//                                  takes its next ceil((limit - valid) * f)
 //                                  ranked candidates
+//     lz_tile_count, nn_prefix,    the round's list grouped by primitive
+//     scan_totals, lz_tile_scatter (longest first) with the nodes in the
+//                                  spatial order of dpg_expand (tiles of 256
+//                                  Z-ordered nodes), so the lockstep warps
+//                                  see neighbouring nodes as in a full expand
 //     exact check of the list      the persistent lockstep warps of
 //                                  check_kernels.cuh, results written to the
 //                                  candidates' own rows
@@ -40,7 +45,6 @@ using namespace dpg;
 namespace {
 
 struct LazyCounters {
-  unsigned long long list_n;    // pairs listed this round
   unsigned long long checked;   // pairs checked this round (lz_update)
   unsigned long long valid;     // valid verdicts among them
   unsigned long long accepted;  // accepted in total
@@ -156,27 +160,61 @@ __global__ void __launch_bounds__(kSortThreads) lz_sort(const uint32_t *off, uin
   }
 }
 
-// nodes short of `limit` valid motions list their next ranked candidates
-__global__ void lz_select(int64_t N, const uint32_t *off, const uint32_t *rank, const uint32_t *cur,
-                          uint32_t *next, const uint32_t *valid, int limit, float f, const uint32_t *prim,
-                          uint32_t *l_node, uint32_t *l_prim, uint32_t *l_dest, LazyCounters *ctr) {
+// nodes short of `limit` valid motions take their next ranked candidates:
+// ranks [cur, next)
+__global__ void lz_select(int64_t N, const uint32_t *off, const uint32_t *cur, uint32_t *next, const uint32_t *valid,
+                          int limit, float f) {
   const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (v >= N) return;
-  const uint32_t b = off[v], seg = off[v + 1] - b, c = cur[v];
+  const uint32_t seg = off[v + 1] - off[v], c = cur[v];
   if ((int)valid[v] >= limit || c >= seg) {
     next[v] = c;
     return;
   }
   const uint32_t want = (uint32_t)ceilf((float)(limit - (int)valid[v]) * f);
-  const uint32_t m = min(seg - c, max(want, 1u));
-  const unsigned long long base = atomicAdd(&ctr->list_n, (unsigned long long)m);
-  for (uint32_t r = 0; r < m; r++) {
-    const uint32_t idx = rank[b + c + r];
-    l_node[base + r] = (uint32_t)v;
-    l_prim[base + r] = prim[idx];
-    l_dest[base + r] = idx;
+  next[v] = c + min(seg - c, max(want, 1u));
+}
+
+// Tiles of 256 nodes in processing order (perm: position -> node, or the
+// identity): per tile, how many of the round's candidates each primitive
+// has (table[tile][P]).
+__global__ void __launch_bounds__(256) lz_tile_count(int64_t N, const uint32_t *perm, const uint32_t *off,
+                                                     const uint32_t *rank, const uint32_t *cur, const uint32_t *next,
+                                                     const uint32_t *prim, int P, uint32_t *table) {
+  extern __shared__ uint32_t hist[];
+  for (int i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0u;
+  __syncthreads();
+  const int64_t pos = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (pos < N) {
+    const uint32_t v = perm ? perm[pos] : (uint32_t)pos, b = off[v];
+    for (uint32_t r = cur[v]; r < next[v]; r++) atomicAdd(&hist[prim[rank[b + r]]], 1u);
   }
-  next[v] = c + m;
+  __syncthreads();
+  uint32_t *t = table + (int64_t)blockIdx.x * P;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) t[i] = hist[i];
+}
+
+// the round's list: entry at pbase[p] + (tile prefix) + (rank in the tile);
+// within a tile the order is arbitrary (the nodes of a tile are neighbours)
+__global__ void __launch_bounds__(256) lz_tile_scatter(int64_t N, const uint32_t *perm, const uint32_t *off,
+                                                       const uint32_t *rank, const uint32_t *cur,
+                                                       const uint32_t *next, const uint32_t *prim, int P,
+                                                       const uint32_t *table, const unsigned long long *pbase,
+                                                       uint32_t *l_node, uint32_t *l_dest) {
+  extern __shared__ uint32_t hist[];
+  for (int i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0u;
+  __syncthreads();
+  const int64_t pos = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (pos < N) {
+    const uint32_t v = perm ? perm[pos] : (uint32_t)pos, b = off[v];
+    const uint32_t *t = table + (int64_t)blockIdx.x * P;
+    for (uint32_t r = cur[v]; r < next[v]; r++) {
+      const uint32_t idx = rank[b + r], p = prim[idx];
+      const unsigned long long slot = pbase[p] + t[p] + atomicAdd(&hist[p], 1u);
+      l_node[slot] = v;
+      l_dest[slot] = idx;
+    }
+  }
 }
 
 // the first `limit` valid candidates in rank order are accepted
@@ -247,7 +285,7 @@ extern "C" int dpg_lazy_check(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N
       (rc = ctx_ensure(c, c->lz_off, 4 * (Nz + 1))) || (rc = ctx_ensure(c, c->lz_cnt, 4 * Nz)) ||
       (rc = ctx_ensure(c, c->lz_cur, 4 * Nz)) || (rc = ctx_ensure(c, c->lz_next, 4 * Nz)) ||
       (rc = ctx_ensure(c, c->lz_valid, 4 * Nz)) || (rc = ctx_ensure(c, c->lz_rank, 4 * nz)) ||
-      (rc = ctx_ensure(c, c->lz_lnode, 4 * nz)) || (rc = ctx_ensure(c, c->lz_lprim, 4 * nz)) ||
+      (rc = ctx_ensure(c, c->lz_lnode, 4 * nz)) ||
       (rc = ctx_ensure(c, c->lz_ldest, 4 * nz)) || (rc = ctx_ensure(c, c->lz_ctr, sizeof(LazyCounters))))
     return rc;
   if (!c->h_lz) {
@@ -302,19 +340,34 @@ extern "C" int dpg_lazy_check(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N
   po.min_gap = out->min_gap;
   po.flags = out->flags;
   const CheckArgs ca = ctx_check_args(c, prec, opts->contact_band, nv, po);
+  // processing order of the nodes and the per-tile primitive table
+  const uint32_t *perm = nullptr;
+  if ((rc = ctx_spatial_order(c, x_dev, N, st, &perm))) return rc;
+  const int64_t tiles = (N + 255) / 256;
+  const size_t hsm = sizeof(uint32_t) * (size_t)P;
+  if (hsm > 200 * 1024) return ctx_fail(c, DPG_ERR_ARG, "lazy_check: more than 51200 primitives");
+  if ((rc = ctx_ensure(c, c->lz_table, sizeof(uint32_t) * (size_t)P * tiles)) ||
+      (rc = ctx_ensure(c, c->tot, sizeof(uint32_t) * P)) || (rc = ctx_ensure(c, c->pbase, 8 * (size_t)P)) ||
+      (rc = ctx_ensure(c, c->ord_pbase, 8 * ((size_t)P + 1))) || (rc = ctx_ensure(c, c->ord_ibase, 8 * ((size_t)P + 1))))
+    return rc;
+  cudaFuncSetAttribute(lz_tile_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
+  cudaFuncSetAttribute(lz_tile_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
+  uint32_t *table = P_<uint32_t>(c->lz_table), *tot = P_<uint32_t>(c->tot);
+  unsigned long long *pbase = P_<unsigned long long>(c->pbase);
   float f = score_dev ? 1.25f : 2.5f;
   int rounds = 0;
   long long n_checked = 0, n_valid = 0, n_recheck = 0;
   for (;;) {
     cudaMemsetAsync(d_lz, 0, sizeof(LazyCounters), st);
-    lz_select<<<gN, 256, 0, st>>>(N, off, rank, cur, nxt, valid, limit, f, prim_dev, P_<uint32_t>(c->lz_lnode),
-                                  P_<uint32_t>(c->lz_lprim), P_<uint32_t>(c->lz_ldest), d_lz);
-    if ((rc = sync_counters())) return rc;
-    const int64_t m = (int64_t)h_lz->list_n;
-    if (m == 0) break;
-    if ((rc = ctx_check_list(c, prec, ca, m, P_<uint32_t>(c->lz_lnode), P_<uint32_t>(c->lz_lprim),
-                             P_<uint32_t>(c->lz_ldest), st, false)))
-      return rc;
+    cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), st);
+    lz_select<<<gN, 256, 0, st>>>(N, off, cur, nxt, valid, limit, f);
+    lz_tile_count<<<(unsigned)tiles, 256, hsm, st>>>(N, perm, off, rank, cur, nxt, prim_dev, P, table);
+    nn_prefix<<<(unsigned)((P + 31) / 32), 256, 0, st>>>(P, (int)tiles, table, tot);
+    scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), tot, pbase, P_<unsigned long long>(c->ord_pbase),
+                                    P_<unsigned long long>(c->ord_ibase), n, c->d_ctr);
+    lz_tile_scatter<<<(unsigned)tiles, 256, hsm, st>>>(N, perm, off, rank, cur, nxt, prim_dev, P, table, pbase,
+                                                        P_<uint32_t>(c->lz_lnode), P_<uint32_t>(c->lz_ldest));
+    if ((rc = ctx_check_grouped(c, prec, ca, P_<uint32_t>(c->lz_lnode), P_<uint32_t>(c->lz_ldest), st))) return rc;
     lz_update<<<gN, 256, 0, st>>>(N, off, rank, cur, nxt, valid, limit, out->verdict, out->flags, d_lz);
     if (cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st) != cudaSuccess)
       return ctx_fail(c, DPG_ERR_CUDA, "lazy_check: counters");
@@ -325,9 +378,9 @@ extern "C" int dpg_lazy_check(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N
     n_recheck += (long long)c->h_ctr->n_recheck;
     st_out.n_accepted += (int64_t)h_lz->accepted;
     if (c->h_ctr->status == DPG_ERR_ABORTED) return ctx_fail(c, DPG_ERR_ABORTED, "lazy_check: aborted");
-    if (h_lz->active == 0) break;
+    if (h_lz->active == 0 || h_lz->checked == 0) break;
     // next round: as many candidates as the last round's yield suggests
-    const double yield = h_lz->checked ? (double)h_lz->valid / (double)h_lz->checked : 0.0;
+    const double yield = (double)h_lz->valid / (double)h_lz->checked;
     f = (float)std::clamp(yield > 0 ? 1.15 / yield : 16.0, 1.0, 16.0);
   }
   st_out.n_checked = n_checked;

@@ -8,7 +8,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import ExpandOpts, ExpandOut, LazyStats, RobotDesc, check
+from ._lib import ExpandOpts, ExpandOut, LazyStats, RobotDesc, TuneReport, Tuning, check
 
 VALID, COLLISION, OUT_OF_BOUNDS = 0, 1, 2
 
@@ -222,6 +222,30 @@ class Context:
         return dict(n_checked=int(st.n_checked), n_valid=int(st.n_valid), n_accepted=int(st.n_accepted),
                     rounds=int(st.rounds), max_candidates=int(st.max_candidates),
                     n_contact_recheck=int(out.n_contact_recheck))
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        check(self.lib.dpg_get_tuning(self.h, C.byref(t)), self.h)
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        """launch choices (dpg_tuning fields); results never depend on them"""
+        t = Tuning(**{**self.tuning(), **kw})
+        check(self.lib.dpg_set_tuning(self.h, C.byref(t)), self.h)
+
+    def autotune(self, x_ptr: int, N: int, radius: float, precision: int = 0, reps: int = 3,
+                 cache_path: str | None = None) -> dict:
+        """dpg_autotune on the N device-resident states at x_ptr: times the
+        launch choices, applies the fastest; returns the report."""
+        opts = ExpandOpts(radius=radius, precision=precision, x_on_device=1, out_on_device=1, mode=0,
+                          contact_band=1e-4, ball_band=1e-5)
+        r = TuneReport()
+        check(self.lib.dpg_autotune(self.h, C.byref(opts), N, C.c_void_p(x_ptr), reps,
+                                    cache_path.encode() if cache_path else None, C.byref(r)), self.h)
+        tdict = lambda t: {k: getattr(t, k) for k, _ in Tuning._fields_}
+        return {"chosen": tdict(r.chosen), "initial": tdict(r.initial), "ms_chosen": r.ms_chosen,
+                "ms_initial": r.ms_initial, "seconds": r.seconds, "candidates": r.candidates,
+                "from_cache": bool(r.from_cache), "key": r.key.decode()}
 
     def timings(self):
         t = (C.c_double * 4)()

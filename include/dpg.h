@@ -268,6 +268,19 @@ int dpg_lazy_check(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const d
 int dpg_expand_noalloc(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x_dev,
                        dpg_expand_out *out);
 
+/* Launch choices of a context (defaults in brackets); dpg_autotune picks
+ * them per workload (dpg_tune.h).  Results never depend on them. */
+#define DPG_CHECK_LOCKSTEP 0 /* the 32 lanes of a warp walk their pairs' states and candidates */
+#define DPG_CHECK_SLOTS 1    /* per chunk of states, (lane, candidate) slots spread over the warp */
+typedef struct dpg_tuning {
+  int32_t check_variant;       /* DPG_CHECK_* [DPG_CHECK_SLOTS]; FP64_STRICT always walks lockstep */
+  int32_t check_blocks_per_sm; /* resident check blocks per SM, 0 = the occupancy maximum [0] */
+  int32_t grid_min_nodes;      /* batches from this size scan the ball through the key grid [2048] */
+  int32_t pipe_launches;       /* check launches of a host-output expand, 1..8 [8] */
+} dpg_tuning;
+int dpg_get_tuning(const dpg_ctx *ctx, dpg_tuning *t);
+int dpg_set_tuning(dpg_ctx *ctx, const dpg_tuning *t);
+
 /* Wait for the context's stream. */
 int dpg_sync(dpg_ctx *ctx);
 /* Raise (1) or clear (0) the abort flag polled by the device work queue. */

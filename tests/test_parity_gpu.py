@@ -25,10 +25,12 @@ def gpu(dpg_lib):
     return G
 
 
-def run_gpu(G, wl, precision, **kw):
+def run_gpu(G, wl, precision, tuning=None, **kw):
     with G.Context(wl.robot) as ctx:
         ctx.upload_primitives(wl.prims)
         ctx.upload_env(wl.env)
+        if tuning:
+            ctx.set_tuning(**tuning)
         return ctx.expand(wl.nodes, wl.radius, precision=precision, **kw)
 
 
@@ -57,6 +59,20 @@ def test_parity_seeded(gpu, cfg, scale, precision):
     assert ora["n_pairs"] > 0
     # the fast baseline carries no min_gap; compare that on the plain oracle below
     compare(wl.robot.kind, res, ora, precision, min_gap=False)
+
+
+@pytest.mark.parametrize("cfg,scale", [(1, 0.1), (2, 0.02), (3, 0.01), (5, 0.01)])
+@pytest.mark.parametrize("tuning", [
+    {"check_variant": 0}, {"check_variant": 1, "check_blocks_per_sm": 2},
+    {"check_variant": 1, "grid_min_nodes": 1 << 30, "pipe_launches": 3}])
+def test_parity_under_tuning(gpu, cfg, scale, tuning):
+    """Every launch choice of dpg_set_tuning gives the oracle's results:
+    the lockstep check, the slot-parallel check at another occupancy, the
+    ball scan without the key grid and another pipeline depth (host outputs)."""
+    wl = W.make_workload(cfg, scale=scale, seed=177 + cfg)
+    res = run_gpu(gpu, wl, 0, tuning)
+    ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius)
+    compare(wl.robot.kind, res, ora, 0)
 
 
 @pytest.mark.parametrize("cfg", [1, 2, 3, 5])
