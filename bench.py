@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--dropin-nodes", type=int, default=2000, help="nodes of the per-node drop-in arm")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch choices (no autotuner)")
+    ap.add_argument("--tuning", default="", help="launch choices to apply instead of the autotuner, "
+                    "e.g. check_variant=0,check_blocks_per_sm=3 (dpg_tuning fields)")
     ap.add_argument("--arm-envs", type=int, default=40, help="training environments of the surrogate arm")
     ap.add_argument("--no-extras", action="store_true",
                     help="headline workload only: no expansion arms, no other workloads (profiling runs)")
@@ -460,7 +462,10 @@ def run_ours(args, rank, world, local_rank):
 
     # ---------------- launch choices: the project's autotuner on this batch
     tune = None
-    if not args.no_tune:
+    if args.tuning:
+        ctx.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tuning.split(","))})
+        tune = {"chosen": ctx.tuning(), "source": "--tuning"}
+    elif not args.no_tune:
         x_t = torch.from_numpy(wl.nodes).to(f"cuda:{dev}")
         torch.cuda.synchronize()
         tune = ctx.autotune(x_t.data_ptr(), N, wl.radius, precision=prec)
@@ -988,8 +993,22 @@ def ctypes_peak(lib, dev):
     return v.value if rc == 0 else float("nan")
 
 
+def spawn_ranks(args):
+    """`--gpus N` outside torchrun: start N ranks of this script on one node
+    (127.0.0.1 rendezvous) and return their exit status."""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(spawn_ranks(args))
     rank, world, local_rank = dist_info()
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -99,6 +99,7 @@ SIGNATURES = [
                                  C.POINTER(LazyStats)]),
     ("dpg_get_tuning", C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     ("dpg_set_tuning", C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    ("dpg_mlp_wait_selftest", C.c_int, [C.c_int, C.c_uint32]),
     ("dpg_sync", C.c_int, [C.c_void_p]),
     # include/dpg_tune.h
     ("dpg_autotune", C.c_int, [C.c_void_p, C.POINTER(ExpandOpts), C.c_int64, C.c_void_p, C.c_int32, C.c_char_p,

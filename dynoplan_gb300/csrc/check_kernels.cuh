@@ -29,6 +29,8 @@
 // on the spot, so verdicts equal the FP64 oracle's.
 #pragma once
 
+#include <type_traits>
+
 #include "expand_kernels.cuh"
 
 namespace dpg {
@@ -466,7 +468,8 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
 
 template <int CH, int PARTS> struct SlotScratch {
   Pose<float> pose[CH * PARTS];  // the chunk's pose rows, [j * PARTS + q]
-  unsigned mg[32][CH];           // per lane and state: min axis-aligned gap (order-preserving bits)
+  float4 aabb[CH * PARTS];       // planar robots: (centre x, centre y, half x, half y) of each part
+  unsigned mg[CH][32];           // per state and lane: min axis-aligned gap (order-preserving bits)
   unsigned hit[32];              // per lane: bit j = contact at state k0 + j
   unsigned rc[32];               // per lane: bit j = a test at k0 + j was decided in FP64
 };
@@ -644,10 +647,15 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
     if (T > 0) {
       if (lane < CH * PARTS) {
         const int j = lane / PARTS, q = lane % PARTS;
-        if (k0 + j < L) S.pose[lane] = pose[(int64_t)q * pv.S + s0 + k0 + j];
+        if (k0 + j < L) {
+          const Pose<float> ps = pose[(int64_t)q * pv.S + s0 + k0 + j];
+          S.pose[lane] = ps;
+          const float ac = fabsf(ps.c), as = fabsf(ps.s);
+          S.aabb[lane] = make_float4(ps.cx, ps.cy, hl * ac + hw * as, hl * as + hw * ac);
+        }
       }
 #pragma unroll
-      for (int j = 0; j < CH; j++) S.mg[lane][j] = ord_gap(INFINITY);
+      for (int j = 0; j < CH; j++) S.mg[j][lane] = ord_gap(INFINITY);
       S.hit[lane] = 0u;
       S.rc[lane] = 0u;
       __syncwarp();
@@ -681,32 +689,41 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
           }
           if (o >= 0 && o < n_obs) {
             const double *ox64 = A.nv.x64 + (int64_t)onode * R::NX;
+            using Ob = std::conditional_t<R::SPHERE, Obs3<float>, Obs2<float>>;
+            const Ob ob = ((const Ob *)obs_sm)[o];
             for (int j = 0; j < onst; j++) {
               const int k = k0 + j;
-              const float tk = float(k) * dt;
               float sx = osh[0], sy = osh[1], sz = 0.f;
               if (V) {
+                const float tk = float(k) * dt;
                 sx += tk * osh[D + 0];
                 sy += tk * osh[D + 1];
-              }
-              if (D == 3) {
+                if (D == 3) sz = osh[2] + tk * osh[D + 2];
+              } else if (D == 3) {
                 sz = osh[2];
-                if (V) sz += tk * osh[D + 2];
               }
               float g = INFINITY;
               bool hit = false;
 #pragma unroll
               for (int q = 0; q < PARTS; q++) {
-                const Pose<float> ps = S.pose[j * PARTS + q];
                 int r;
                 if constexpr (R::SPHERE) {
-                  const Obs3<float> ob = ((const Obs3<float> *)obs_sm)[o];
+                  const Pose<float> ps = S.pose[j * PARTS + q];
                   r = sphere_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c + sz, ob, rad, band, g);
                 } else {
-                  const Obs2<float> ob = ((const Obs2<float> *)obs_sm)[o];
-                  const float ac = fabsf(ps.c), as = fabsf(ps.s);
-                  r = planar_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c, ps.s, hl * ac + hw * as,
-                                               hl * as + hw * ac, ob, hl, hw, band, g);
+                  // axis-aligned reject first; the oriented axes only within the band
+                  const float4 bb = S.aabb[j * PARTS + q];
+                  const float dx = bb.x + sx - ob.cx, dy = bb.y + sy - ob.cy;
+                  const float ga = fmaxf(fabsf(dx) - (bb.z + ob.hx), fabsf(dy) - (bb.w + ob.hy));
+                  g = fminf(g, ga);
+                  if (ga > band) {
+                    r = 0;
+                  } else {
+                    const Pose<float> ps = S.pose[j * PARTS + q];
+                    float unused = INFINITY;
+                    r = planar_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c, ps.s, bb.z, bb.w, ob, hl, hw, band,
+                                                 unused);
+                  }
                 }
                 if (r == 2) {  // decide in FP64
                   r = gap64<KIND>(A, s0, k, q, ox64, o) <= 0.0 ? 1 : 0;
@@ -714,7 +731,8 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
                 }
                 hit |= r == 1;
               }
-              atomicMin(&S.mg[owner][j], ord_gap(g));
+              // gaps above the cap are reported as +inf: only smaller ones are merged
+              if (g <= kGapCap) atomicMin(&S.mg[j][owner], ord_gap(g));
               if (hit) {
                 atomicOr(&S.hit[owner], 1u << j);
                 break;  // later states of this candidate lie past the lane's first contact
@@ -727,7 +745,7 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
       if (nst > 0) {
         const unsigned h = S.hit[lane];
         const int last = h ? __ffs(h) - 1 : nst - 1;
-        for (int j = 0; j <= last; j++) mg = fminf(mg, unord_gap(S.mg[lane][j]));
+        for (int j = 0; j <= last; j++) mg = fminf(mg, unord_gap(S.mg[j][lane]));
         if (S.rc[lane] & (last >= 31 ? 0xffffffffu : ((2u << last) - 1u))) rechecked = true;
         if (h) {
           collided = true;
@@ -820,7 +838,8 @@ __device__ void load_obstacles(const EnvView &ev, void *sm) {
 // SLOTS: the slot-parallel narrow phase (FP32 tests with the band, NW > 0);
 // its per-warp scratch follows the obstacles at A.slot_offset.
 template <int KIND, class Real, bool BAND, int NW, bool ES64 = false, bool SLOTS = false>
-__global__ void __launch_bounds__(kCheckThreads, Robot<KIND>::CHECK_BLOCKS) check_pairs(CheckArgs A) {
+__global__ void __launch_bounds__(kCheckThreads, SLOTS ? Robot<KIND>::SLOT_BLOCKS : Robot<KIND>::CHECK_BLOCKS)
+    check_pairs(CheckArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   load_obstacles<Real, KIND>(A.ev, smem);
   const int lane = threadIdx.x & 31;

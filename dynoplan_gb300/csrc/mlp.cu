@@ -134,6 +134,54 @@ extern "C" int dpg_gemm_bf16(const void *A_dev, const void *B_dev, float *C_dev,
 }
 
 // ---------------------------------------------------------------------------
+// Failure path of the bounded waits (dpg_mlp_wait_selftest): the protocol of
+// the tensor-core kernels -- TMEM allocated by warp 0, mbarriers initialised
+// by thread 0, a bounded wait, on give-up an error word and the TMEM freed --
+// with nothing issued that could complete the barrier, so the wait runs out
+// with no copy or MMA in flight.
+namespace {
+
+__global__ void __launch_bounds__(128) wait_selftest(int *err, uint32_t polls) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  if (threadIdx.x == 0) {
+    umma::mbar_init(&bar, 1);
+    umma::mbar_fence_init();
+  }
+  if (threadIdx.x < 32) {
+    umma::tmem_alloc(&tslot, 32);
+    umma::tmem_relinquish();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  // the consumer's wait: no producer arrives on `bar`
+  const bool ok = threadIdx.x == 0 ? umma::mbar_wait(&bar, 0, polls) : true;
+  const bool bad = __syncthreads_or(!ok);
+  if (bad && threadIdx.x == 0) atomicExch(err, 1);
+  umma::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) umma::tmem_dealloc(tslot, 32);
+}
+
+}  // namespace
+
+extern "C" int dpg_mlp_wait_selftest(int device, uint32_t polls) {
+  if (polls == 0 || polls > (1u << 24)) return DPG_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return DPG_ERR_NODEVICE;
+  int *err = nullptr;
+  if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return DPG_ERR_OOM;
+  cudaMemset(err, 0, sizeof(int));
+  wait_selftest<<<1, 128>>>(err, polls);
+  int h = 0;
+  const cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  if (e != cudaSuccess) return DPG_ERR_CUDA;
+  return h ? DPG_ERR_TIMEOUT : DPG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // The surrogate MLP (include/dpg_mlp.h).
 #include <cmath>
 #include <vector>

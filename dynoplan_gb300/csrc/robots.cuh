@@ -42,6 +42,7 @@ template <> struct Robot<DPG_ROBOT_UNICYCLE1> {
   static constexpr int KEYD = 1;  // kept key components: theta
   static constexpr int CHUNK = 8;  // states per culling chunk
   static constexpr int CHECK_BLOCKS = 4;  // check_pairs blocks per SM (register bound)
+  static constexpr int SLOT_BLOCKS = 4;  // slot-parallel check: 64 registers a thread
   __host__ __device__ static int key_comp(int i) { return 2; }
   __host__ __device__ static int vel_comp(int i) { return -1; }
 };
@@ -52,6 +53,7 @@ template <> struct Robot<DPG_ROBOT_CAR1> {
   static constexpr int KEYD = 2;  // theta0, theta1
   static constexpr int CHUNK = 8;
   static constexpr int CHECK_BLOCKS = 4;  // measured: 4 beats 3, 5 and 6 here
+  static constexpr int SLOT_BLOCKS = 4;  // slot-parallel check: 64 registers a thread
   __host__ __device__ static int key_comp(int i) { return 2 + i; }
   __host__ __device__ static int vel_comp(int i) { return -1; }
 };
@@ -62,6 +64,7 @@ template <> struct Robot<DPG_ROBOT_QUAD2D> {
   static constexpr int KEYD = 2;  // theta, w
   static constexpr int CHUNK = 16;  // dt 0.01: ten times the states of the others per second
   static constexpr int CHECK_BLOCKS = 4;
+  static constexpr int SLOT_BLOCKS = 4;  // slot-parallel check: 64 registers a thread
   __host__ __device__ static int key_comp(int i) { return i == 0 ? 2 : 5; }
   __host__ __device__ static int vel_comp(int i) { return 3 + i; }
 };
@@ -72,6 +75,7 @@ template <> struct Robot<DPG_ROBOT_QUAD3D> {
   static constexpr int KEYD = 7;  // quaternion (4), w (3)
   static constexpr int CHUNK = 16;
   static constexpr int CHECK_BLOCKS = 5;  // measured: 5 beats 4 and 6 here
+  static constexpr int SLOT_BLOCKS = 4;  // slot-parallel check: 64 registers a thread
   __host__ __device__ static int key_comp(int i) { return i < 4 ? 3 + i : 6 + i; }
   __host__ __device__ static int vel_comp(int i) { return 7 + i; }
 };

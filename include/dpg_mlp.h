@@ -34,6 +34,13 @@ extern "C" {
 int dpg_gemm_bf16(const void *A_dev, const void *B_dev, float *C_dev, int M, int N, int K, int impl,
                   int split_k);
 
+/* Failure path of the bounded mbarrier waits of the tensor-core kernels: one
+ * CTA allocates tensor memory, waits with at most `polls` polls on an
+ * mbarrier that nothing will complete (no copy or MMA is issued), records
+ * the timeout, frees the tensor memory and returns.  Returns DPG_ERR_TIMEOUT
+ * when the wait gave up, as it must; the device stays usable. */
+int dpg_mlp_wait_selftest(int device, uint32_t polls);
+
 /* ---- the surrogate MLP --------------------------------------------------
  * Input row per (node, primitive) pair (96 bf16): normalised node state (16,
  * zero padded), 8x8 occupancy patch around the node (64), the primitive's

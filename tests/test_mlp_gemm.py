@@ -59,3 +59,16 @@ def test_tma_gemm_matches_reference(dpg_lib, M, N, K, split):
     c_tc, exact, mag = _run(dpg_lib, torch, M, N, K, 2, split=split)
     bad = np.abs(c_tc - exact) > 1e-3 * mag + 1e-5
     assert not bad.any(), f"{bad.sum()} of {bad.size} differ; first {np.argwhere(bad)[:4].tolist()}"
+
+
+def test_bounded_wait_gives_up_and_device_stays_usable(dpg_lib):
+    """The bounded mbarrier wait of the tensor-core kernels, made to run out:
+    nothing completes the barrier (no copy or MMA is issued), the wait gives
+    up after its polls, the kernel records the timeout, frees its tensor
+    memory and returns DPG_ERR_TIMEOUT; the next tensor-core GEMM runs."""
+    torch = pytest.importorskip("torch")
+    from dynoplan_gb300 import _lib
+    for _ in range(2):
+        assert dpg_lib.dpg_mlp_wait_selftest(0, 4096) == _lib.DPG_ERR_TIMEOUT
+    got, ref, mag = _run(dpg_lib, torch, 256, 64, 128, 2)
+    assert (np.abs(got - ref) <= 1e-3 * mag + 1e-5).all()
