@@ -176,6 +176,7 @@ __device__ __forceinline__ bool near_box(const float *cen, const float *hf, cons
   }
 }
 
+
 // ------------------------------------------------------------- one pair ----
 
 // NW: words of the per-lane obstacle bitmasks (obstacles <= 32 NW); 0 = no

@@ -31,6 +31,8 @@ struct dpg_ctx {
   std::vector<int64_t> h_soff, h_aoff, h_coff;
   DevBuf len, soff, aoff, order, key32, kconst32, st64, st32, act64, pose32, pose64, pbox, pbox32;
   DevBuf coff, cbox32, tbox32;
+  // reverse ball (tdb-A*'s reverse search): keys of each primitive's last state
+  DevBuf rkey32, rkconst32, rkrow;
   // key-space grid of the primitives (robots with one or two key components)
   DevBuf kg_start, kg_tab;
   dpg::KeyGrid kg{};  // n0 = 0: no grid

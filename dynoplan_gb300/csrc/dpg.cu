@@ -81,6 +81,7 @@ RobotParams to_params(const dpg_robot_desc &r) {
 }
 
 int pos_dim(int kind) { return kind == DPG_ROBOT_QUAD3D ? 3 : 2; }
+
 int key_dim(int kind) {
   switch (kind) {
     case DPG_ROBOT_UNICYCLE1: return Robot<DPG_ROBOT_UNICYCLE1>::KEYD;
@@ -178,14 +179,14 @@ static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
 template <int KIND>
 static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv, double radius, double ball_band,
                         int64_t Wpad, int64_t B, int64_t W, uint32_t *mask, uint32_t *cnt, uint32_t *tot,
-                        DevCounters *ctr, cudaStream_t st) {
+                        DevCounters *ctr, cudaStream_t st, bool allow_grid = true) {
   using R = Robot<KIND>;
   const RobotParams &rp = c->rp;
   const int P = pv.P;
   const float4 w32 = make_float4((float)rp.w[0], (float)rp.w[1], (float)rp.w[2], (float)rp.w[3]);
   bool done = false;
   if constexpr (R::KEYD <= 2) {
-    if (c->kg.n0 > 0 && nv.N >= c->tune.grid_min_nodes) {
+    if (allow_grid && c->kg.n0 > 0 && nv.N >= c->tune.grid_min_nodes) {
       // half-width of the cell range along a key component: radius plus band
       // over its weight, widened; -1 = every cell
       auto half = [&](double wk, bool periodic) -> float {
@@ -321,7 +322,7 @@ void dpg_destroy(dpg_ctx *c) {
                     &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill,
                     &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_rank, &c->ord_tiles, &c->x64s,
                     &c->kg_start, &c->kg_tab, &c->lz_off, &c->lz_cnt, &c->lz_cur, &c->lz_next, &c->lz_valid,
-                    &c->lz_rank, &c->lz_lnode, &c->lz_ldest, &c->lz_ctr, &c->lz_table};
+                    &c->lz_rank, &c->lz_lnode, &c->lz_ldest, &c->lz_ctr, &c->lz_table, &c->rkey32, &c->rkconst32, &c->rkrow};
   for (DevBuf *b : bufs) release(*b);
   if (c->d_ctr) cudaFree(c->d_ctr);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
@@ -457,14 +458,19 @@ static int load_tables(dpg_ctx *c, int32_t P, const int32_t *len, const double *
       (rc = ensure(c, c->pbox32, sizeof(float) * 2 * pd * P)) ||
       (rc = ensure(c, c->coff, sizeof(int64_t) * P)) ||
       (rc = ensure(c, c->cbox32, sizeof(float) * 2 * pd * NC)) ||
-      (rc = ensure(c, c->tbox32, sizeof(float) * 2 * pd * P)))
+      (rc = ensure(c, c->tbox32, sizeof(float) * 2 * pd * P)) ||
+      (rc = ensure(c, c->rkey32, sizeof(float) * kd * P)) || (rc = ensure(c, c->rkconst32, sizeof(float) * P)) ||
+      (rc = ensure(c, c->rkrow, sizeof(int64_t) * P)))
     return rc;
+  std::vector<int64_t> last_row(P);
+  for (int p = 0; p < P; p++) last_row[p] = c->h_soff[p] + len[p] - 1;
   cudaStream_t st = c->stream;
   CUDA_TRY(c, cudaMemcpyAsync(c->len.p, len, sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->soff.p, c->h_soff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->aoff.p, c->h_aoff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->order.p, c->h_order.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->coff.p, c->h_coff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->rkrow.p, last_row.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->st64.p, states, sizeof(double) * nx * S, copy, st));
   if (A > 0) CUDA_TRY(c, cudaMemcpyAsync(c->act64.p, actions, sizeof(double) * nu * A, copy, st));
   const RobotParams rp = c->rp;
@@ -481,6 +487,9 @@ static int load_tables(dpg_ctx *c, int32_t P, const int32_t *len, const double *
                                                        P_<double>(c->st64), P_<float>(c->key32),
                                                        P_<float>(c->kconst32), P_<double>(c->pbox),
                                                        P_<float>(c->pbox32));
+    build_keys<KIND><<<(P + 127) / 128, 128, 0, st>>>(rp, P, P_<int32_t>(c->len), P_<int64_t>(c->rkrow),
+                                                       P_<double>(c->st64), P_<float>(c->rkey32),
+                                                       P_<float>(c->rkconst32), nullptr, nullptr, true);
     build_chunks<KIND><<<(P + 127) / 128, 128, 0, st>>>(rp, P, P_<int32_t>(c->len), P_<int64_t>(c->soff),
                                                          P_<int64_t>(c->coff), P_<Pose<double>>(c->pose64), S,
                                                          P_<float>(c->cbox32), P_<float>(c->tbox32));
@@ -644,6 +653,11 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     return fail(c, DPG_ERR_ARG, "expand: bad radius or precision");
   if (out->capacity < 0 || out->capacity > (int64_t)0xffffffffLL)
     return fail(c, DPG_ERR_ARG, "expand: capacity out of range");
+  const bool reverse = (opts->mode & DPG_MODE_REVERSE) != 0;
+  if (reverse && !(opts->mode & DPG_MODE_BALL_ONLY))
+    return fail(c, DPG_ERR_ARG, "expand: DPG_MODE_REVERSE gives the reverse ball only (with DPG_MODE_BALL_ONLY)");
+  if (reverse && c->robot.kind != DPG_ROBOT_UNICYCLE1 && c->robot.kind != DPG_ROBOT_CAR1)
+    return fail(c, DPG_ERR_ARG, "expand: the reverse ball is defined for unicycle1 and car1");
   if (*(volatile int *)c->h_abort) return fail(c, DPG_ERR_ABORTED, "expand: abort flag raised");
   CUDA_TRY(c, cudaSetDevice(c->device));
   const int kind = c->robot.kind, nx = c->robot.nx, P = c->P;
@@ -743,6 +757,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   pv.S = c->S;
   pv.len = P_<int32_t>(c->len);
   pv.soff = P_<int64_t>(c->soff);
+  pv.krow = P_<int64_t>(c->soff);
   pv.order = P_<int32_t>(c->order);
   pv.key32 = P_<float>(c->key32);
   pv.kconst32 = P_<float>(c->kconst32);
@@ -755,6 +770,11 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   pv.coff = P_<int64_t>(c->coff);
   pv.cbox32 = P_<float>(c->cbox32);
   pv.tbox32 = P_<float>(c->tbox32);
+  if (reverse) {  // the ball keys on each primitive's last state (the key grid holds start keys)
+    pv.key32 = P_<float>(c->rkey32);
+    pv.kconst32 = P_<float>(c->rkconst32);
+    pv.krow = P_<int64_t>(c->rkrow);
+  }
   NodeView nv{N, P_<double>(c->x64), P_<float>(c->nkey32), P_<float>(c->noff32)};
   EnvView ev{};
   ev.dim = c->dim;
@@ -811,7 +831,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     if (N > 0) {
       prep_nodes<KIND><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(nv);
       launch_ball<KIND>(c, pv, nv, opts->radius, ball_band, Wpad, B, W, P_<uint32_t>(c->mask),
-                        P_<uint32_t>(c->cnt), P_<uint32_t>(c->tot), ctr, st);
+                        P_<uint32_t>(c->cnt), P_<uint32_t>(c->tot), ctr, st, !reverse);
     } else {
       cudaMemsetAsync(c->tot.p, 0, sizeof(uint32_t) * P, st);
     }
@@ -997,6 +1017,7 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
     return fail(c, DPG_ERR_ARG, "noalloc: bad radius or precision");
   if (out->capacity < 0 || out->capacity > (int64_t)0xffffffffLL)
     return fail(c, DPG_ERR_ARG, "noalloc: capacity out of range");
+  if (opts->mode & DPG_MODE_REVERSE) return fail(c, DPG_ERR_ARG, "noalloc: no reverse ball (use dpg_expand)");
   if (*(volatile int *)c->h_abort) return fail(c, DPG_ERR_ABORTED, "noalloc: abort flag raised");
   CUDA_TRY(c, cudaSetDevice(c->device));
   const int kind = c->robot.kind, P = c->P;
@@ -1043,6 +1064,7 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
   pv.S = c->S;
   pv.len = P_<int32_t>(c->len);
   pv.soff = P_<int64_t>(c->soff);
+  pv.krow = P_<int64_t>(c->soff);
   pv.order = P_<int32_t>(c->order);
   pv.key32 = P_<float>(c->key32);
   pv.kconst32 = P_<float>(c->kconst32);
@@ -1169,6 +1191,7 @@ PrimView ctx_prim_view(dpg_ctx *c) {
   pv.S = c->S;
   pv.len = P_<int32_t>(c->len);
   pv.soff = P_<int64_t>(c->soff);
+  pv.krow = P_<int64_t>(c->soff);
   pv.order = P_<int32_t>(c->order);
   pv.key32 = P_<float>(c->key32);
   pv.kconst32 = P_<float>(c->kconst32);

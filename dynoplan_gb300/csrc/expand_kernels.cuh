@@ -63,6 +63,7 @@ struct PrimView {
   int64_t S;                 // state rows
   const int32_t *len;        // [P]
   const int64_t *soff;       // [P] first state row
+  const int64_t *krow;       // [P] row of the state the ball test keys on (first; last in reverse)
   const int32_t *order;      // [P] primitive ids, decreasing length
   const float *key32;        // [KEYD][P] kept key components, angles wrapped
   const float *kconst32;     // [P] constant part of the metric
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(kNNThreads) nn_mask(RobotParams rp, PrimView p
           in = d <= radius;
           if (fabsf(d - radius) <= band) {  // decide in FP64
             const int p = p0 + j;
-            const double d64 = key_dist64<KIND>(rp, nv.x64 + n * R::NX, pv.st64 + pv.soff[p] * R::NX);
+            const double d64 = key_dist64<KIND>(rp, nv.x64 + n * R::NX, pv.st64 + pv.krow[p] * R::NX);
             in = d64 <= radius64;
             rechecks++;
           }
@@ -421,7 +422,7 @@ __global__ void __launch_bounds__(kNNThreads) nn_grid(RobotParams rp, PrimView p
             bool in = d <= radius;
             const int p = __float_as_int(t[u].w);
             if (fabsf(d - radius) <= band) {  // decide in FP64
-              in = key_dist64<KIND>(rp, xn, pv.st64 + pv.soff[p] * R::NX) <= radius64;
+              in = key_dist64<KIND>(rp, xn, pv.st64 + pv.krow[p] * R::NX) <= radius64;
               rechecks++;
             }
             if (in) {
@@ -625,8 +626,11 @@ __global__ void build_poses(RobotParams rp, int64_t S, const double *st64, Pose<
 // Per primitive: key components (angles wrapped), constant metric part,
 // swept position box of the canonical states.
 template <int KIND>
+// keys_only: just the key tables (soff then gives each primitive's key row,
+// e.g. its last state for the reverse ball)
 __global__ void build_keys(RobotParams rp, int P, const int32_t *len, const int64_t *soff,
-                           const double *st64, float *key32, float *kconst32, double *pbox, float *pbox32) {
+                           const double *st64, float *key32, float *kconst32, double *pbox, float *pbox32,
+                           bool keys_only = false) {
   using R = Robot<KIND>;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
@@ -646,6 +650,7 @@ __global__ void build_keys(RobotParams rp, int P, const int32_t *len, const int6
          rp.w[2] * sqrt(s[7] * s[7] + s[8] * s[8] + s[9] * s[9]);
   }
   kconst32[p] = (float)kc;
+  if (keys_only) return;
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
   for (int k = 0; k < len[p]; k++)
     for (int i = 0; i < R::POSD; i++) {

@@ -154,15 +154,18 @@ class Context:
 
     def expand(self, x: np.ndarray, radius: float, precision: int = 0, capacity: int | None = None,
                contact_band: float = 1e-4, ball_band: float = 1e-5, outputs=None,
-               ball_only: bool = False) -> ExpandResult:
+               ball_only: bool = False, reverse: bool = False) -> ExpandResult:
         """Batched expand of the rows of x (N x nx), results in host arrays.
-        ball_only: the in-ball (node, prim) pairs without the exact check."""
+        ball_only: the in-ball (node, prim) pairs without the exact check;
+        reverse (with ball_only): the reverse ball, motions keyed on their
+        last state (tdb-A*'s reverse search)."""
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, self.nx)
         N = len(x)
         if capacity is None:
             capacity = max(1024, N * 64)
         opts = ExpandOpts(radius=radius, precision=precision, x_on_device=0, out_on_device=0,
-                          mode=1 if ball_only else 0, contact_band=contact_band, ball_band=ball_band)
+                          mode=(1 if ball_only else 0) | (2 if reverse else 0), contact_band=contact_band,
+                          ball_band=ball_band)
         while True:
             es_dtype = np.float64 if precision != 0 else np.float32
             o = outputs if outputs is not None else dict(

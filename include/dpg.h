@@ -81,6 +81,14 @@ extern "C" {
 
 /* dpg_expand_opts.mode */
 #define DPG_MODE_BALL_ONLY 1
+/* with DPG_MODE_BALL_ONLY: the reverse ball of tdb-A*'s reverse search --
+ * motions keyed on their LAST state (position included) tested against the
+ * node's canonical state, the tree nigh_factory_t builds for
+ * reverse_search (include/dynoplan/nigh_custom_spaces.hpp:575-693, used at
+ * src/tdbastar/tdbastar.cpp:575-576 and tdbastar.hpp:255); unicycle1 and
+ * car1, the robots that factory covers.  Check the pairs with
+ * dpg_tdb_check_pairs (reverse = 1). */
+#define DPG_MODE_REVERSE 2
 
 /* per-pair flags */
 #define DPG_FLAG_CONTACT_RECHECK 1 /* verdict recomputed in FP64 (contact/bounds band) */

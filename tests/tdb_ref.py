@@ -63,3 +63,21 @@ def check(m, prims, env, x, node_g, node, prim, reverse, c_time, c_state, goal, 
                     break
         out.append((v, fi))
     return np.array(out, np.int64).reshape(-1, 2)
+
+
+def reverse_ball(m, prims, nodes, radius):
+    """tdb-A*'s reverse neighbours (nigh_factory_t with reverse_search,
+    include/dynoplan/nigh_custom_spaces.hpp:575-693, queried at
+    include/dynoplan/tdbastar/tdbastar.hpp:255): motion p is a neighbour of
+    node x when distance(canonical(x), last state of p) <= radius; the
+    canonical state zeroes the position, the motion's key keeps its own.
+    Returns the sorted (node, prim) keys node * 2^32 + prim."""
+    keys = []
+    for n, x in enumerate(nodes):
+        c = np.array(x, float)
+        c[:2] = 0.0
+        for p in range(prims.P):
+            xs, _ = prims.motion(p)
+            if ob.distance(m, c, xs[-1]) <= radius:
+                keys.append(n * (1 << 32) + p)
+    return np.sort(np.array(keys, np.int64))

@@ -219,3 +219,31 @@ def test_full_size_quadrotor_determinism(gpu):
     ka, ks = key(a, sel), key(s, np.ones(s["n_pairs"], bool))
     for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap", "flags"):
         np.testing.assert_array_equal(a[k][sel][ka], s[k][ks])
+
+
+@pytest.mark.parametrize("kind", [W.UNICYCLE1, W.CAR1, W.QUAD3D])
+@pytest.mark.parametrize("variant", [0, 1])
+def test_obstacle_grid_border_cases(gpu, kind, variant):
+    """The obstacle grid that level-1 culling reads: obstacles straddling the
+    bounds, lying wholly outside them, and tiny ones; nodes along the
+    border so trajectories leave the bounds.  Every result equals the
+    oracle's, for both narrow phases."""
+    m = W.robot_model(kind)
+    dim = 3 if kind == W.QUAD3D else 2
+    rng = np.random.default_rng(11 + kind)
+    ext = np.array([6.0, 6.0, 3.0][:dim])
+    lo = rng.uniform(-1.0, ext + 1.0, (60, dim))
+    side = rng.uniform(0.01, 1.2, (60, dim))
+    obs_lo, obs_hi = lo - 0.5 * side, lo + 0.5 * side
+    env = W.Env(np.zeros(dim), ext, obs_lo, obs_hi)
+    nodes = W.make_nodes(m, W.Env(np.zeros(dim), ext, obs_lo[:0], obs_hi[:0]), 600, seed=5)
+    nodes[:200, 0] = rng.choice([0.05, ext[0] - 0.05], 200)       # along two edges
+    prims = W.make_primitives(m, 60, 5 if dim == 2 else 20, 40 if dim == 2 else 120, seed=3)
+    with gpu.Context(m) as ctx:
+        ctx.upload_primitives(prims)
+        ctx.upload_env(env)
+        ctx.set_tuning(check_variant=variant)
+        res = ctx.expand(nodes, 0.6)
+    ora = ob.expand(m, prims, env, nodes, 0.6)
+    assert ora["n_pairs"] > 0 and (ora["verdict"] == 2).any() and (ora["verdict"] == 1).any()
+    compare(kind, res, ora, 0)

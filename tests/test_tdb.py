@@ -74,3 +74,45 @@ def test_tdb_rejects_reverse_for_rollout_robots(dpg_lib):
         ctx.upload_env(wl.env)
         with pytest.raises(DpgError):
             T.check_pairs(ctx, wl.nodes, [0], [0], reverse=True)
+
+
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_reverse_ball_matches_restatement(dpg_lib, cfg):
+    """The reverse ball (DPG_MODE_REVERSE): motions keyed on their last
+    state against the node's canonical state; identical pair sets to the
+    restatement over the oracle's metric, for a small and a spatially
+    ordered batch, and its pairs check like tdb-A*'s reverse pairs."""
+    import tdb_ref
+    from dynoplan_gb300 import gpu as G
+    from dynoplan_gb300 import tdb as T
+    wl = W.make_workload(cfg, scale=0.03, seed=70 + cfg)
+    m = wl.robot
+    radius = 0.6   # the last states lie away from the origin: a wider ball than the forward one
+    for nodes in (wl.nodes[:150], np.concatenate([wl.nodes] * (1 + 2100 // len(wl.nodes)))[:2100]):
+        with G.Context(m) as ctx:
+            ctx.upload_primitives(wl.prims)
+            ctx.upload_env(wl.env)
+            r = ctx.expand(nodes, radius, ball_only=True, reverse=True)
+            got = np.sort(r["node"].astype(np.int64) * (1 << 32) + r["prim"].astype(np.int64))
+            if len(nodes) <= 150:
+                v, fi, _ = T.check_pairs(ctx, nodes, r["node"], r["prim"], reverse=True)
+        ref = tdb_ref.reverse_ball(m, wl.prims, nodes[:150] if len(nodes) > 150 else nodes, radius)
+        if len(nodes) > 150:
+            got = got[got < 150 * (1 << 32)]
+        else:
+            refc = tdb_ref.check(m, wl.prims, wl.env, nodes, np.zeros(len(nodes), np.float32), r["node"], r["prim"],
+                                 True, np.zeros(0), np.zeros((0, m.nx)), nodes[0], 0.3)
+            assert np.array_equal(v.astype(np.int64), refc[:, 0]) and np.array_equal(fi.astype(np.int64), refc[:, 1])
+        assert len(ref) > 0
+        np.testing.assert_array_equal(got, ref)
+
+
+def test_reverse_ball_refused_for_rollout_robots(dpg_lib):
+    from dynoplan_gb300 import gpu as G
+    from dynoplan_gb300._lib import DpgError
+    wl = W.make_workload(5, scale=0.005)
+    with G.Context(wl.robot) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        with pytest.raises(DpgError):
+            ctx.expand(wl.nodes, 0.5, ball_only=True, reverse=True)
