@@ -51,6 +51,13 @@ L2_FLUSH_BYTES = 512 << 20
 # (dram__bytes_read.sum + dram__bytes_write.sum over the pairs of the captured
 # launch), per workload; scaled to the bench's launch by its checked pairs.
 # Workloads without a capture report traffic null.
+# Instruction issue of the check kernel from the same ncu capture
+# (profiles/check_pairs_car1_50k.md): sm__inst_executed.avg.per_cycle_active
+# over the SM's 4 issue slots per cycle, and warp instructions per pair.
+CHECK_ISSUE = {
+    2: {"inst_per_cycle": 2.916, "issue_slots": 4, "warp_instructions_per_pair": 1306890404 / 4126228,
+        "active_lanes_per_instruction": 13.93},
+}
 CHECK_TRAFFIC_PER_PAIR = {
     2: (36.005632e6 + 63.423488e6) / 4126228,  # ncu capture (slot variant), car1_v0 with 50,000 nodes
 }
@@ -369,7 +376,11 @@ def check_roofline(lib, wl, m, dev, cfg):
             "work_model": "FP32 ops of the culling algorithm as run, no idle-lane waste "
                           "(bench.algorithmic_check_ops; 4000-pair sample, scaled)",
             "lower_bound_ops_per_launch": alg_lower,
-            "lower_bound_tflops": alg_lower / m["check_s"] / 1e12}
+            "lower_bound_tflops": alg_lower / m["check_s"] / 1e12,
+            **({"issue": {**CHECK_ISSUE[cfg], "frac": CHECK_ISSUE[cfg]["inst_per_cycle"] / CHECK_ISSUE[cfg]["issue_slots"],
+                          "source": "ncu capture of the same kernel, profiles/check_pairs_car1_50k.md; the kernel "
+                                    "is bound by instruction issue, not by FP32 arithmetic or DRAM"}}
+               if cfg in CHECK_ISSUE else {})}
 
 
 def cpu_baseline(wl, seconds):
@@ -431,6 +442,22 @@ def other_workload(args, lib, G, cfg, dev):
         rec["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds / 2)
         rec["vs_cpu_all_cores"] = rec["value"] / rec["cpu_baseline"]["value"]
     return rec
+
+
+def tune_small_set(lib, G, W, dev):
+    """The autotuner on car1 with a 400-primitive set (the primitive count of
+    the reference's car1 db-A* configuration) over the bench's nodes:
+    chosen choice, its check+ball time and the default's."""
+    import torch
+    wl = W.make_workload(2)
+    prims = W.make_primitives(wl.robot, 400, 5, 100, seed=2400)
+    with G.Context(wl.robot, device=dev) as ctx:
+        ctx.upload_primitives(prims)
+        ctx.upload_env(wl.env)
+        x = torch.from_numpy(wl.nodes).to(f"cuda:{dev}")
+        torch.cuda.synchronize()
+        rep = ctx.autotune(x.data_ptr(), len(wl.nodes), wl.radius, precision=0)
+    return {"primitives": 400, "nodes": len(wl.nodes), "tuning": rep}
 
 
 def run_ours(args, rank, world, local_rank):
@@ -515,6 +542,8 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and args.config == 2 and not args.no_extras:
         for cfg in (1, 3):
             others[W.CONFIGS[cfg]["name"]] = other_workload(args, lib, G, cfg, dev)
+        if not args.no_tune:
+            others["car1_v0, 400 primitives (autotuner only)"] = tune_small_set(lib, G, W, dev)
     if rank != 0:
         return
     line = {

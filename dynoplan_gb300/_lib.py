@@ -52,7 +52,7 @@ class ExpandOpts(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("check_variant", C.c_int32), ("check_blocks_per_sm", C.c_int32),
-                ("grid_min_nodes", C.c_int32), ("pipe_launches", C.c_int32)]
+                ("grid_min_nodes", C.c_int32), ("pipe_launches", C.c_int32), ("direct_host", C.c_int32)]
 
 
 class TuneReport(C.Structure):

@@ -51,9 +51,10 @@ struct CheckArgs {
   // double->float conversions at 1/64 of the FP32 rate)
   float dt32, half_len32, half_wid32, radius32, band32;
   float lo32[3], hi32[3];
-  // this launch takes work items [n_items sub / nsub, n_items (sub + 1) / nsub)
-  // (nsub 0 = 1: all items)
+  // this launch takes work items [n_items cum[sub] / cum[nsub],
+  // n_items cum[sub + 1] / cum[nsub]) (integer weights; nsub <= 1: all items)
   int sub, nsub;
+  int sub_cum[kMaxSub + 1];
   // when set, the pair's node id is written back through it (processing
   // order -> caller's numbering) once the pair is checked
   const uint32_t *perm;
@@ -412,6 +413,10 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
   else { verdict = DPG_VALID; fi = L; }
   const int er = first_oob < L ? first_oob : L - 1;  // end-state row
   const int64_t row_out = o.out_index ? (int64_t)o.out_index[pair] : pair;
+  if (o.node_host) {
+    o.node_host[row_out] = A.perm ? A.perm[node] : node;
+    o.prim_host[row_out] = (uint32_t)p;
+  }
   if (o.verdict) o.verdict[row_out] = verdict;
   if (o.first_invalid) o.first_invalid[row_out] = (int16_t)fi;
   if (o.min_gap)
@@ -777,6 +782,10 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
   else { verdict = DPG_VALID; fi = L; }
   const int er = first_oob < L ? first_oob : L - 1;  // end-state row
   const int64_t row_out = o.out_index ? (int64_t)o.out_index[pair] : pair;
+  if (o.node_host) {
+    o.node_host[row_out] = A.perm ? A.perm[node] : node;
+    o.prim_host[row_out] = (uint32_t)p;
+  }
   if (o.verdict) o.verdict[row_out] = verdict;
   if (o.first_invalid) o.first_invalid[row_out] = (int16_t)fi;
   if (o.min_gap)
@@ -847,7 +856,8 @@ __global__ void __launch_bounds__(kCheckThreads, SLOTS ? Robot<KIND>::SLOT_BLOCK
   const int P = A.pv.P;
   const unsigned long long n_all = A.ctr->n_items;
   const int nsub = A.nsub > 0 ? A.nsub : 1;
-  const unsigned long long i_lo = n_all * A.sub / nsub, n_items = n_all * (A.sub + 1) / nsub;
+  const unsigned long long i_lo = nsub > 1 ? n_all * A.sub_cum[A.sub] / A.sub_cum[nsub] : 0ull;
+  const unsigned long long n_items = nsub > 1 ? n_all * A.sub_cum[A.sub + 1] / A.sub_cum[nsub] : n_all;
   while (true) {
     unsigned long long item = 0;
     int stop = 0;

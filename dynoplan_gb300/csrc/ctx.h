@@ -67,7 +67,7 @@ struct dpg_ctx {
   int *d_abort = nullptr;
   // launch choices (dpg_set_tuning): check variant, blocks per SM, the batch
   // size from which the ball scan uses the key grid, pipelined check launches
-  dpg_tuning tune{DPG_CHECK_SLOTS, 0, 2048, 8};
+  dpg_tuning tune{DPG_CHECK_SLOTS, 0, 2048, 8, 0};
   cudaEvent_t ev[6] = {};
   double timings[4] = {0, 0, 0, 0};
 };

@@ -176,6 +176,19 @@ static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
 // same mask and counts.
 // (an expand whose results go to host buffers runs tune.pipe_launches <=
 // kMaxSub check launches, one work-queue counter each)
+
+// Cumulative item weights of the pipelined check launches: each range
+// 3/4 the size of the one before, so a range's result copy (about half as
+// long as its check on car1) overlaps the next range's check and the last,
+// exposed copy is small.  cum[0] = 0, cum[n] = the total.
+static void pipe_weights(int n, int *cum) {
+  cum[0] = 0;
+  double w = 1000.0;
+  for (int j = 0; j < n; j++) {
+    cum[j + 1] = cum[j] + (int)w;
+    w *= 0.75;
+  }
+}
 template <int KIND>
 static void launch_ball(const dpg_ctx *c, const PrimView &pv, const NodeView &nv, double radius, double ball_band,
                         int64_t Wpad, int64_t B, int64_t W, uint32_t *mask, uint32_t *cnt, uint32_t *tot,
@@ -638,7 +651,7 @@ int dpg_set_tuning(dpg_ctx *c, const dpg_tuning *t) {
   if (!c || !t) return DPG_ERR_ARG;
   if ((t->check_variant != DPG_CHECK_LOCKSTEP && t->check_variant != DPG_CHECK_SLOTS) ||
       t->check_blocks_per_sm < 0 || t->check_blocks_per_sm > 32 || t->grid_min_nodes < 0 ||
-      t->pipe_launches < 1 || t->pipe_launches > kMaxSub)
+      t->pipe_launches < 1 || t->pipe_launches > kMaxSub || (t->direct_host != 0 && t->direct_host != 1))
     return fail(c, DPG_ERR_ARG, "set_tuning: value out of range");
   c->tune = *t;
   return DPG_OK;
@@ -720,10 +733,39 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     pv_out.flags = out->flags ? P_<uint8_t>(c->p_flags) : nullptr;
   }
 
+  // host outputs in page-locked memory the GPU maps (dpg_host_alloc,
+  // cudaHostAlloc, cudaHostRegister): the check kernel writes every result
+  // there itself, node ids and primitives included, so no copy follows it
+  bool direct = false;
+  if (!dev_out && c->tune.direct_host && !(opts->mode & DPG_MODE_BALL_ONLY) && cap > 0) {
+    void *hp[7] = {out->node, out->prim, out->verdict, out->first_invalid, out->end_state, out->min_gap, out->flags};
+    void *dp[7] = {};
+    direct = out->node && out->prim;
+    for (int i = 0; i < 7 && direct; i++) {
+      if (!hp[i]) continue;
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, hp[i]) != cudaSuccess || at.type != cudaMemoryTypeHost || !at.devicePointer) {
+        cudaGetLastError();
+        direct = false;
+      } else {
+        dp[i] = at.devicePointer;
+      }
+    }
+    if (direct) {
+      pv_out.node_host = static_cast<uint32_t *>(dp[0]);
+      pv_out.prim_host = static_cast<uint32_t *>(dp[1]);
+      pv_out.verdict = static_cast<uint8_t *>(dp[2]);
+      pv_out.first_invalid = static_cast<int16_t *>(dp[3]);
+      pv_out.end_state = dp[4];
+      pv_out.min_gap = static_cast<float *>(dp[5]);
+      pv_out.flags = static_cast<uint8_t *>(dp[6]);
+    }
+  }
+
   // host-buffer outputs of a checked batch in spatial order: the check runs as
   // tune.pipe_launches launches over item ranges and each range's results are copied out
   // while the next range is checked
-  const bool pipelined = !dev_out && !(opts->mode & DPG_MODE_BALL_ONLY) && reorder && cap > 0;
+  const bool pipelined = !dev_out && !direct && !(opts->mode & DPG_MODE_BALL_ONLY) && reorder && cap > 0;
   if (pipelined) {
     if (!c->cstream) {
       CUDA_TRY(c, cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
@@ -868,6 +910,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       // the previous range's last items leave idle
       ca.perm = reorder ? P_<uint32_t>(c->ord_perm) : nullptr;
       ca.nsub = pipelined ? c->tune.pipe_launches : 1;
+      pipe_weights(ca.nsub, ca.sub_cum);
       for (int j = 0; j < ca.nsub; j++) {
         ca.sub = j;
         cudaStream_t s = pipelined && (j & 1) ? c->xstream : st;
@@ -905,8 +948,10 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
           {out->first_invalid, c->p_fi.p, 2}, {out->end_state, c->p_end.p, es_bytes * nx},
           {out->min_gap, c->p_gap.p, 4}, {out->flags, c->p_flags.p, 1}};
       const int np = c->tune.pipe_launches;
+      int cum[kMaxSub + 1];
+      pipe_weights(np, cum);
       for (int j = 0; j < np; j++) {
-        const int64_t a = pair_at(h0.n_items * j / np), e = pair_at(h0.n_items * (j + 1) / np);
+        const int64_t a = pair_at(h0.n_items * cum[j] / cum[np]), e = pair_at(h0.n_items * cum[j + 1] / cum[np]);
         CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev_sub[j], 0));
         if (e > a)
           for (const auto &f : cp)
@@ -931,7 +976,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   const int64_t np = (int64_t)h.n_pairs;
   if (pipelined) {
     // copied above
-  } else if (!dev_out && np > 0) {
+  } else if (!dev_out && !direct && np > 0) {
     struct { void *dst; void *src; size_t b; } cp[] = {
         {out->node, c->p_node.p, 4}, {out->prim, c->p_prim.p, 4}, {out->verdict, c->p_verdict.p, 1},
         {out->first_invalid, c->p_fi.p, 2}, {out->end_state, c->p_end.p, es_bytes * nx},

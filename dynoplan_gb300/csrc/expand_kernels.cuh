@@ -104,6 +104,9 @@ struct PairView {
   float *min_gap;
   uint8_t *flags;
   const uint32_t *out_index;  // when set, results of pair i go to row out_index[i]
+  // when set (host arrays the GPU writes directly), the check also writes
+  // each pair's caller node id and primitive there
+  uint32_t *node_host, *prim_host;
 };
 
 __device__ __forceinline__ float wrap_pi_f64(double a) {

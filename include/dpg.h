@@ -285,6 +285,10 @@ typedef struct dpg_tuning {
   int32_t check_blocks_per_sm; /* resident check blocks per SM, 0 = the occupancy maximum [0] */
   int32_t grid_min_nodes;      /* batches from this size scan the ball through the key grid [2048] */
   int32_t pipe_launches;       /* check launches of a host-output expand, 1..8 [8] */
+  int32_t direct_host;         /* host outputs in page-locked memory the GPU can map: the check
+                                  kernel writes them itself, no staging copies (1), or the staged,
+                                  pipelined copies (0) [0: on the GB300 hosts measured, the
+                                  kernel's stores over the host link doubled the check time] */
 } dpg_tuning;
 int dpg_get_tuning(const dpg_ctx *ctx, dpg_tuning *t);
 int dpg_set_tuning(dpg_ctx *ctx, const dpg_tuning *t);

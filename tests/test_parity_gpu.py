@@ -247,3 +247,36 @@ def test_obstacle_grid_border_cases(gpu, kind, variant):
     ora = ob.expand(m, prims, env, nodes, 0.6)
     assert ora["n_pairs"] > 0 and (ora["verdict"] == 2).any() and (ora["verdict"] == 1).any()
     compare(kind, res, ora, 0)
+
+
+@pytest.mark.parametrize("cfg,scale,precision", [(2, 0.03, 0), (2, 0.005, 0), (1, 0.3, 1), (3, 0.05, 0)])
+def test_direct_host_writes(gpu, cfg, scale, precision):
+    """Outputs in page-locked host memory: the check kernel writes them itself
+    (direct_host = 1) -- the same rows as the staged, pipelined copies
+    (direct_host = 0) and the oracle's results; small batches (caller's node
+    order) and spatially ordered ones."""
+    wl = W.make_workload(cfg, scale=scale, seed=810 + cfg)
+    N, nx = wl.nodes.shape
+    res = {}
+    with gpu.Context(wl.robot) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        n = ctx.expand(wl.nodes, wl.radius, precision=precision)["n_pairs"]
+        cap = n + 64
+        for direct in (1, 0):
+            ctx.set_tuning(direct_host=direct)
+            pins = {"node": gpu.PinnedArray(cap, np.uint32), "prim": gpu.PinnedArray(cap, np.uint32),
+                    "verdict": gpu.PinnedArray(cap, np.uint8), "first_invalid": gpu.PinnedArray(cap, np.int16),
+                    "end_state": gpu.PinnedArray((cap, nx), np.float64 if precision else np.float32),
+                    "min_gap": gpu.PinnedArray(cap, np.float32), "flags": gpu.PinnedArray(cap, np.uint8)}
+            for v in pins.values():
+                v.array[...] = 0x5A if v.array.dtype.itemsize == 1 else 7   # stale values must not survive
+            r = ctx.expand(wl.nodes, wl.radius, precision=precision, capacity=cap,
+                           outputs={k: v.array for k, v in pins.items()})
+            res[direct] = {k: (np.array(v) if isinstance(v, np.ndarray) else v) for k, v in r.items()}
+            for v in pins.values():
+                v.free()
+    for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap", "flags"):
+        np.testing.assert_array_equal(res[1][k], res[0][k])
+    ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius, fast=True, threads=ob.lib().orc_max_threads())
+    compare(wl.robot.kind, res[1], ora, precision, min_gap=False)
