@@ -917,7 +917,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
         launch_check<KIND>(c, ca, prec, s);
         if (pipelined) cudaEventRecord(c->ev_sub[j], s);
       }
-      if (pipelined) {  // join: the last launch on the second stream
+      if (pipelined && ca.nsub > 1) {  // join: the last launch on the second stream
         const int last_x = ca.nsub % 2 == 0 ? ca.nsub - 1 : ca.nsub - 2;
         cudaStreamWaitEvent(st, c->ev_sub[last_x], 0);
       }

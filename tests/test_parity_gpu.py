@@ -64,7 +64,7 @@ def test_parity_seeded(gpu, cfg, scale, precision):
 @pytest.mark.parametrize("cfg,scale", [(1, 0.1), (2, 0.02), (3, 0.01), (5, 0.01)])
 @pytest.mark.parametrize("tuning", [
     {"check_variant": 0}, {"check_variant": 1, "check_blocks_per_sm": 2},
-    {"check_variant": 1, "grid_min_nodes": 1 << 30, "pipe_launches": 3}])
+    {"check_variant": 1, "grid_min_nodes": 1 << 30, "pipe_launches": 3}, {"pipe_launches": 1}])
 def test_parity_under_tuning(gpu, cfg, scale, tuning):
     """Every launch choice of dpg_set_tuning gives the oracle's results:
     the lockstep check, the slot-parallel check at another occupancy, the
