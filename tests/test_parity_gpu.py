@@ -61,7 +61,7 @@ def test_parity_seeded(gpu, cfg, scale, precision):
     compare(wl.robot.kind, res, ora, precision, min_gap=False)
 
 
-@pytest.mark.parametrize("cfg,scale", [(1, 0.1), (2, 0.02), (3, 0.01), (5, 0.01)])
+@pytest.mark.parametrize("cfg,scale", [(1, 0.1), (2, 0.02), (2, 0.03), (3, 0.01), (5, 0.01)])
 @pytest.mark.parametrize("tuning", [
     {"check_variant": 0}, {"check_variant": 1, "check_blocks_per_sm": 2},
     {"check_variant": 1, "grid_min_nodes": 1 << 30, "pipe_launches": 3}, {"pipe_launches": 1}])
