@@ -211,7 +211,7 @@ struct dpg_mlp {
   float *out = nullptr, *loss = nullptr;
   int *err = nullptr;
   int step = 0;
-  int fused = 1;  // forward through mlp_forward_fused when the tensor maps can be made
+  int fused = 2;  // forward kernel: 2 mlp_forward_fused2, 1 mlp_forward_fused, 0 layer GEMMs
   int sm_count = 0;
   // training-step inputs copied to fixed buffers, hyper-parameters in device
   // memory [lr, ctg_weight, 1 - b1^t, 1 - b2^t]: the step is captured once
@@ -444,12 +444,19 @@ int dpg_mlp_forward(dpg_mlp *M, const void *node_feat_dev, const uint32_t *node_
   if (fused) {  // one persistent kernel, one CTA per SM
     FusedArgs fa{nf, M->emb16, node_dev, prim_dev, M->w[DPG_MLP_B1], M->w[DPG_MLP_B2], M->w[DPG_MLP_B3],
                  M->w[DPG_MLP_B4], out_dev, n, M->err};
-    if (cudaFuncSetAttribute(mlp_forward_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem) !=
-        cudaSuccess)
-      return DPG_ERR_CUDA;
     const int64_t tiles = (n + 127) / 128;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, std::max(M->sm_count, 1));
-    mlp_forward_fused<<<grid, kFusedThreads, kFusedSmem, st>>>(tw[0], tw[1], tw[2], tw[3], fa);
+    if (M->fused == 2) {  // warp-specialised: epilogues overlap the next layer's MMAs
+      if (cudaFuncSetAttribute(mlp_forward_fused2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFused2Smem) !=
+          cudaSuccess)
+        return DPG_ERR_CUDA;
+      mlp_forward_fused2<<<grid, kFused2Threads, kFused2Smem, st>>>(tw[0], tw[1], tw[2], tw[3], fa);
+    } else {
+      if (cudaFuncSetAttribute(mlp_forward_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem) !=
+          cudaSuccess)
+        return DPG_ERR_CUDA;
+      mlp_forward_fused<<<grid, kFusedThreads, kFusedSmem, st>>>(tw[0], tw[1], tw[2], tw[3], fa);
+    }
     if (cudaGetLastError() != cudaSuccess) return DPG_ERR_CUDA;
     flops = forward_flops(pad128(n));
   }
@@ -600,7 +607,8 @@ int dpg_mlp_train_step(dpg_mlp *M, const void *node_feat_dev, const uint32_t *no
 
 int dpg_mlp_set_fused(dpg_mlp *M, int fused) {
   if (!M) return DPG_ERR_ARG;
-  M->fused = fused != 0;
+  if (fused < 0 || fused > 2) return DPG_ERR_ARG;
+  M->fused = fused;
   return DPG_OK;
 }
 

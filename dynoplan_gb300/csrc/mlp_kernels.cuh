@@ -494,4 +494,246 @@ static __global__ void __launch_bounds__(kFusedThreads, 1)
   if (warp == 0) umma::tmem_dealloc(tmem, 256);
 }
 
+
+// ---------------------------------------------------------------------------
+// The same forward, warp-specialised so that the input gather and each
+// layer's epilogue overlap the MMAs.  Warps 0-15 run the epilogues, warp 16
+// (one lane) streams W1..W3 by TMA through a 3-stage ring of 64-column
+// K-chunks (10 chunks a tile, each stage freed as its MMAs complete), warp
+// 17 (one lane) issues the MMAs, warps 18-25 gather the next tile's input
+// rows into their own buffer while the current tile is computed.  The
+// epilogue of layer l writes H_l one 64-column k-block at a time, every warp
+// taking 16 columns of its lane quarter, and each finished k-block releases
+// the MMAs of layer l+1 over it (mbarrier hready[j], 512 arrivals); layers
+// alternate between two TMEM accumulators of 256 columns (512 allocated),
+// so layer l+1 accumulates while layer l's accumulator is still being read.
+// H_l is written over H_{l-1} in place: layer l's MMAs are complete before
+// its epilogue writes (accfull), and layer l+1 reads only k-blocks already
+// written.  The input buffer is refilled once the tile's layer-0 MMAs are
+// complete (xfree).  Every wait is bounded: on expiry the kernel sets *err,
+// waits (bounded) for its copies and MMAs in flight, frees TMEM and returns.
+constexpr int kFused2Threads = 832;  // 16 epilogue warps + TMA warp + MMA warp + 8 gather warps
+constexpr int kF2EpiThreads = 512;
+constexpr int kF2GatherThreads = 256;
+constexpr int kF2Stages = 3;
+constexpr uint32_t kXBytes = 128 * kMlpIn * 2;  // 32 KB: the input rows of a tile
+constexpr size_t kFused2Smem = 1024 + kXBytes + kActBytes + kF2Stages * kWChunk + kW4Bytes + 256;
+
+static __global__ void __launch_bounds__(kFused2Threads, 1)
+    mlp_forward_fused2(const __grid_constant__ CUtensorMap tw1, const __grid_constant__ CUtensorMap tw2,
+                       const __grid_constant__ CUtensorMap tw3, const __grid_constant__ CUtensorMap tw4, FusedArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = umma::smem_u32(smem_raw);
+  unsigned char *xin = smem_raw + ((1024 - (raw & 1023)) & 1023);
+  unsigned char *act = xin + kXBytes;
+  unsigned char *wst = act + kActBytes;             // kF2Stages weight stages
+  unsigned char *w4 = wst + kF2Stages * kWChunk;    // resident W4, 4 k-blocks of 16 rows
+  uint64_t *wfull = reinterpret_cast<uint64_t *>(w4 + kW4Bytes);  // [kF2Stages]
+  uint64_t *wempty = wfull + kF2Stages;                           // [kF2Stages]
+  uint64_t *hready = wempty + kF2Stages;                          // [4]
+  uint64_t *w4full = hready + 4;
+  uint64_t *xready = w4full + 1;
+  uint64_t *xfree = xready + 1;
+  uint64_t *accfull = xfree + 1;
+  uint64_t *drain = accfull + 1;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1);
+  __shared__ __align__(16) float sbias[3][kMlpHidden];
+  __shared__ int s_bad, s_consumed, s_w4_done;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t n_tiles = (a.B + 127) / 128;
+  for (int i = tid; i < 3 * kMlpHidden; i += kFused2Threads)
+    sbias[i / kMlpHidden][i % kMlpHidden] = (i < kMlpHidden ? a.b1 : (i < 2 * kMlpHidden ? a.b2 : a.b3))[i % kMlpHidden];
+  constexpr uint32_t kIdesc = umma::idesc_bf16_f32(128, kMlpHidden);
+  constexpr uint32_t kIdesc4 = umma::idesc_bf16_f32(128, kMlpOutPad);
+  if (tid == 0) {
+    for (int s = 0; s < kF2Stages; s++) {
+      umma::mbar_init(&wfull[s], 1);
+      umma::mbar_init(&wempty[s], 1);
+    }
+    for (int j = 0; j < 4; j++) umma::mbar_init(&hready[j], kF2EpiThreads);
+    umma::mbar_init(w4full, 1);
+    umma::mbar_init(xready, kF2GatherThreads);
+    umma::mbar_init(xfree, 1);
+    umma::mbar_init(accfull, 1);
+    umma::mbar_init(drain, 1);
+    umma::mbar_fence_init();
+    s_bad = 0;
+    s_consumed = 0;
+    s_w4_done = 0;
+  }
+  if (warp == 0) {
+    umma::tmem_alloc(tslot, 512);
+    umma::tmem_relinquish();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  volatile int *bad = &s_bad;
+
+  if (warp == 16) {
+    // ---- TMA producer: W4 once, then W1 (2 chunks), W2, W3 (4 each) per tile
+    if (lane == 0 && blockIdx.x < n_tiles) {
+      const void *wmap[3] = {&tw1, &tw2, &tw3};
+      umma::mbar_arrive_expect_tx(w4full, kW4Bytes);
+      for (int j = 0; j < 4; j++) umma::tma_load_2d(w4 + j * (kMlpOutPad * 128), &tw4, 64 * j, 0, w4full);
+      int cnt = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x)
+        for (int l = 0; l < 3 && ok; l++)
+          for (int j = 0; j < (l == 0 ? kMlpIn : kMlpHidden) / 64; j++, cnt++) {
+            const int s = cnt % kF2Stages;
+            if ((cnt >= kF2Stages && !umma::mbar_wait(&wempty[s], ((cnt / kF2Stages) - 1) & 1)) || *bad) {
+              *bad = 1;
+              ok = false;
+              break;
+            }
+            umma::mbar_arrive_expect_tx(&wfull[s], kWChunk);
+            umma::tma_load_2d(wst + s * kWChunk, wmap[l], 64 * j, 0, &wfull[s]);
+          }
+      // Copies still in flight land before the block's memory goes: once the
+      // MMA thread has stopped (it publishes s_w4_done; waited for at most
+      // ~2 s of SM clock, far beyond any batch), the loads it did not consume
+      // are waited for, bounded.
+      const long long t0 = clock64();
+      while (*(volatile int *)&s_w4_done == 0 && clock64() - t0 < 4000000000ll) {
+      }
+      if (*bad) {
+        const int cons = *(volatile int *)&s_consumed;
+        for (int i = cons; i < cnt; i++) umma::mbar_wait(&wfull[i % kF2Stages], (i / kF2Stages) & 1, 1u << 20);
+      }
+      if (*(volatile int *)&s_w4_done != 2) umma::mbar_wait(w4full, 0, 1u << 20);  // W4 never waited for
+    }
+  } else if (warp == 17) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      int cnt = 0, it = 0;
+      bool w4_ready = false, ok = true, issued_any = false;
+      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, it++) {
+        if (!umma::mbar_wait(xready, it & 1) || *bad) { ok = false; break; }
+        for (int l = 0; l < 4 && ok; l++) {
+          const uint32_t acc = tmem + 256u * (uint32_t)(l & 1);
+          const uint32_t a0 = umma::smem_u32(l == 0 ? xin : act);
+          const int chunks = l == 0 ? kMlpIn / 64 : kMlpHidden / 64;
+          if (l == 3 && !w4_ready) {
+            if (!umma::mbar_wait(w4full, 0)) { ok = false; break; }
+            w4_ready = true;
+          }
+          for (int j = 0; j < chunks; j++) {
+            if (l > 0 && !umma::mbar_wait(&hready[j], (it * 3 + l - 1) & 1)) { ok = false; break; }
+            if (l < 3) {
+              if (!umma::mbar_wait(&wfull[cnt % kF2Stages], (cnt / kF2Stages) & 1)) { ok = false; break; }
+              *(volatile int *)&s_consumed = cnt + 1;
+            }
+            if (*bad) { ok = false; break; }
+            umma::fence_after_sync();
+            const uint32_t ak = a0 + j * (128 * 128);
+            const uint32_t b0 = l < 3 ? umma::smem_u32(wst + (cnt % kF2Stages) * kWChunk)
+                                      : umma::smem_u32(w4 + j * (kMlpOutPad * 128));
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+              umma::mma_bf16(acc, umma::sdesc_kmajor_sw128(ak + kk * 32), umma::sdesc_kmajor_sw128(b0 + kk * 32),
+                             l < 3 ? kIdesc : kIdesc4, (j > 0 || kk > 0) ? 1u : 0u);
+            issued_any = true;
+            if (l < 3) {
+              umma::commit(&wempty[cnt % kF2Stages]);
+              cnt++;
+            }
+          }
+          if (!ok) break;
+          if (l == 0) umma::commit(xfree);  // the input buffer may be refilled once these MMAs are done
+          umma::commit(accfull);
+        }
+      }
+      if (!ok) *bad = 1;
+      if (issued_any) {  // the MMAs issued are complete before the memory goes
+        umma::commit(drain);
+        umma::mbar_wait(drain, 0, 1u << 20);
+      }
+      *(volatile int *)&s_consumed = cnt;
+      __threadfence_block();
+      *(volatile int *)&s_w4_done = w4_ready ? 2 : 1;
+    }
+  } else if (warp >= 18) {
+    // ---- gather warps: the input rows of each tile into xin, once the
+    // previous tile's layer-0 MMAs have read it
+    const int gt = tid - 18 * 32;
+    int it = 0;
+    for (int64_t t = blockIdx.x; t < n_tiles && !*bad; t += gridDim.x, it++) {
+      if (it > 0 && !umma::mbar_wait(xfree, (it - 1) & 1)) { *bad = 1; break; }
+      // two threads a row: the row's indices once, then its eight 16-byte
+      // chunks (node features 0-9, embedding 10-11, zero 12-15) loaded
+      // together before any store
+      static_assert(kF2GatherThreads == 256 && kMlpIn == 128, "two gather threads per row, 8 chunks each");
+      const int r = gt >> 1, c0 = 8 * (gt & 1);
+      const int64_t b = t * 128 + r;
+      uint4 v[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) v[k] = make_uint4(0, 0, 0, 0);
+      if (b < a.B) {
+        const uint4 *nf = reinterpret_cast<const uint4 *>(a.node_feat + (int64_t)a.node[b] * kMlpNodeFeat);
+        const uint4 *em = reinterpret_cast<const uint4 *>(a.emb + (int64_t)a.prim[b] * kMlpEmb);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const int c = c0 + k;
+          if (c < kMlpNodeFeat / 8) v[k] = nf[c];
+          else if (c < (kMlpNodeFeat + kMlpEmb) / 8) v[k] = em[c - kMlpNodeFeat / 8];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 8; k++) *reinterpret_cast<uint4 *>(xin + umma::kmajor_offset(128, r, c0 + k)) = v[k];
+      umma::fence_proxy_async_smem();
+      umma::mbar_arrive(xready);
+    }
+  } else {
+    // ---- epilogue warps: per layer H_l by k-blocks, then the outputs
+    const int q = warp & 3, h = warp >> 2, row = 32 * q + lane;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+    int it = 0;
+    for (int64_t t = blockIdx.x; t < n_tiles && !*bad; t += gridDim.x, it++) {
+      const int64_t m0 = t * 128;
+      bool ok = true;
+      for (int l = 0; l < 3 && ok; l++) {
+        if (!umma::mbar_wait(accfull, (it * 4 + l) & 1)) { *bad = 1; ok = false; break; }
+        umma::fence_after_sync();
+        const uint32_t acc = 256u * (uint32_t)(l & 1);
+        const float *bias = sbias[l];
+        for (int j = 0; j < 4; j++) {
+          const int c0 = 64 * j + 16 * h;
+          float v[16];
+          umma::tmem_ld16(lane_addr + acc + c0, v);
+          __align__(16) __nv_bfloat162 hb[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++)
+            hb[k] = __floats2bfloat162_rn(gelu(v[2 * k] + bias[c0 + 2 * k]), gelu(v[2 * k + 1] + bias[c0 + 2 * k + 1]));
+          *reinterpret_cast<uint4 *>(act + umma::kmajor_offset(128, row, c0 / 8)) = reinterpret_cast<const uint4 *>(hb)[0];
+          *reinterpret_cast<uint4 *>(act + umma::kmajor_offset(128, row, c0 / 8 + 1)) =
+              reinterpret_cast<const uint4 *>(hb)[1];
+          umma::fence_proxy_async_smem();
+          umma::fence_before_sync();
+          umma::mbar_arrive(&hready[j]);
+        }
+      }
+      if (!ok) break;
+      if (!umma::mbar_wait(accfull, (it * 4 + 3) & 1)) { *bad = 1; break; }
+      umma::fence_after_sync();
+      if (h == 0) {
+        float v[16];
+        umma::tmem_ld16(lane_addr + 256u, v);
+        const int64_t b = m0 + row;
+        if (b < a.B) {
+          a.out[b * 2] = v[0] + a.b4[0];
+          a.out[b * 2 + 1] = v[1] + a.b4[1];
+        }
+      }
+      umma::fence_before_sync();
+    }
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (tid == 0 && s_bad) atomicExch(a.err, 1);
+  umma::fence_after_sync();
+  if (warp == 0) umma::tmem_dealloc(tmem, 512);
+}
+
 }  // namespace dpg

@@ -86,10 +86,10 @@ class Surrogate:
                                           lr, ctg_weight, C.byref(loss)))
         return loss.value
 
-    def set_fused(self, fused: bool):
-        """forward through the fused per-tile kernel (default) or the
-        layer-by-layer GEMMs"""
-        check(self.lib.dpg_mlp_set_fused(self.h, 1 if fused else 0))
+    def set_fused(self, fused: int):
+        """forward kernel: 0 the layer-by-layer GEMMs, 1 the fused per-tile
+        kernel, 2 the fused warp-specialised kernel (default)"""
+        check(self.lib.dpg_mlp_set_fused(self.h, int(fused)))
 
     def timing(self):
         ms, fl = C.c_double(), C.c_double()

@@ -79,11 +79,13 @@ int dpg_mlp_train_step(dpg_mlp *mlp, const void *node_feat_dev, const uint32_t *
                        const uint32_t *prim_dev, const float *target_dev, int64_t B, float lr, float ctg_weight,
                        float *loss);
 
-/* Forward kernels: fused != 0 (default) runs the whole MLP per 128-row tile
- * in one persistent tcgen05 kernel (activations kept in shared memory,
- * weights streamed by TMA); fused == 0 runs the layer-by-layer GEMMs the
- * training step uses.  Same arithmetic (bf16 operands, FP32 accumulation in
- * the same order, same epilogue). */
+/* Forward kernels: fused 1 runs the whole MLP per 128-row tile in one
+ * persistent tcgen05 kernel (activations kept in shared memory, weights
+ * streamed by TMA); fused 2 (default) is the same kernel warp-specialised
+ * (a TMA warp, an MMA warp, 16 epilogue warps) so that each layer's
+ * epilogue overlaps the next layer's MMAs; fused 0 runs the layer-by-layer
+ * GEMMs the training step uses.  Same arithmetic (bf16 operands, FP32
+ * accumulation in the same order, same epilogue). */
 int dpg_mlp_set_fused(dpg_mlp *mlp, int fused);
 
 /* device time of the last forward / train step (ms) and the FLOPs it ran */

@@ -122,9 +122,10 @@ def test_fused_forward_matches_layer_by_layer(dpg_lib, B):
     s = Surrogate(P, max_rows=65536, seed=2)
     for k, v in params.items():
         s.set(k, v)
-    s.set_fused(False)
+    s.set_fused(0)
     ref = s.forward(feat_d, node_d, prim_d).cpu().numpy()
-    s.set_fused(True)
-    out = s.forward(feat_d, node_d, prim_d).cpu().numpy()
-    assert out.shape == (B, 2) and np.isfinite(out).all()
-    assert np.abs(out - ref).max() <= 1e-3 * (1 + np.abs(ref).max())
+    for kind in (1, 2):   # one CTA per tile walk; warp-specialised with overlapped epilogues
+        s.set_fused(kind)
+        out = s.forward(feat_d, node_d, prim_d).cpu().numpy()
+        assert out.shape == (B, 2) and np.isfinite(out).all()
+        assert np.abs(out - ref).max() <= 1e-3 * (1 + np.abs(ref).max())
