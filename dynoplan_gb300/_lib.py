@@ -25,6 +25,9 @@ DPG_ERR_NODEVICE = -8
 DPG_UNCHECKED = 255
 DPG_CHECK_LOCKSTEP = 0
 DPG_CHECK_SLOTS = 1
+DPG_HOST_OUT_PIPELINED = 0
+DPG_HOST_OUT_DIRECT = 1
+DPG_HOST_OUT_PROGRESS = 2
 DPG_FLAG_ACCEPTED = 2
 
 DPG_FP32 = 0
@@ -52,7 +55,7 @@ class ExpandOpts(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("check_variant", C.c_int32), ("check_blocks_per_sm", C.c_int32),
-                ("grid_min_nodes", C.c_int32), ("pipe_launches", C.c_int32), ("direct_host", C.c_int32)]
+                ("grid_min_nodes", C.c_int32), ("pipe_launches", C.c_int32), ("host_output", C.c_int32)]
 
 
 class TuneReport(C.Structure):

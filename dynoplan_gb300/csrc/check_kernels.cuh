@@ -55,6 +55,13 @@ struct CheckArgs {
   // n_items cum[sub + 1] / cum[nsub]) (integer weights; nsub <= 1: all items)
   int sub, nsub;
   int sub_cum[kMaxSub + 1];
+  // progress-driven copies (one launch, nsub = 1): the items fall into
+  // n_ranges ranges by the same weights; a warp adds the items it finished
+  // in a range to range_done when it moves to the next range or stops (after
+  // a fence), and the add that completes a range sets range_flag[j] (mapped
+  // host memory) after a system fence
+  int n_ranges;
+  int *range_flag;
   // when set, the pair's node id is written back through it (processing
   // order -> caller's numbering) once the pair is checked
   const uint32_t *perm;
@@ -858,6 +865,23 @@ __global__ void __launch_bounds__(kCheckThreads, SLOTS ? Robot<KIND>::SLOT_BLOCK
   const int nsub = A.nsub > 0 ? A.nsub : 1;
   const unsigned long long i_lo = nsub > 1 ? n_all * A.sub_cum[A.sub] / A.sub_cum[nsub] : 0ull;
   const unsigned long long n_items = nsub > 1 ? n_all * A.sub_cum[A.sub + 1] / A.sub_cum[nsub] : n_all;
+  int cur_range = -1;        // progress-driven copies: the range of this warp's items,
+  unsigned long long cur_cnt = 0;  // and how many of them it finished
+  auto flush_range = [&]() {  // warp-uniform
+    if (cur_cnt == 0) return;
+    __threadfence();  // this lane's result writes, before the count
+    __syncwarp();
+    if (lane == 0) {
+      const int nr = A.n_ranges, tot = A.sub_cum[nr], j = cur_range;
+      const unsigned long long lo = n_all * A.sub_cum[j] / tot;
+      const unsigned long long hi = j + 1 == nr ? n_all : n_all * A.sub_cum[j + 1] / tot;
+      if (atomicAdd(&A.ctr->range_done[j], cur_cnt) + cur_cnt == hi - lo) {
+        __threadfence_system();
+        reinterpret_cast<volatile int *>(A.range_flag)[j] = 1;
+      }
+    }
+    cur_cnt = 0;
+  };
   while (true) {
     unsigned long long item = 0;
     int stop = 0;
@@ -872,6 +896,16 @@ __global__ void __launch_bounds__(kCheckThreads, SLOTS ? Robot<KIND>::SLOT_BLOCK
       break;
     }
     if (item >= n_items) break;
+    if (A.n_ranges > 1) {
+      const int nr = A.n_ranges, tot = A.sub_cum[nr];
+      int j = 0;
+      while (j + 1 < nr && item >= n_all * A.sub_cum[j + 1] / tot) j++;
+      if (j != cur_range) {
+        flush_range();
+        cur_range = j;
+      }
+      cur_cnt++;
+    }
     // order position lo with ord_ibase[lo] <= item < ord_ibase[lo + 1]
     int lo = 0, hi = P;
     while (hi - lo > 1) {
@@ -893,6 +927,7 @@ __global__ void __launch_bounds__(kCheckThreads, SLOTS ? Robot<KIND>::SLOT_BLOCK
       check_one<KIND, Real, BAND, NW, true, ES64>(A, smem, p, (int64_t)pair, node, active);
     }
   }
+  if (A.n_ranges > 1) flush_range();
 }
 
 }  // namespace dpg

@@ -63,11 +63,13 @@ struct dpg_ctx {
   // dpg_lazy_check: candidates by node, ranks, cursors, round lists, counters
   DevBuf lz_off, lz_cnt, lz_cur, lz_next, lz_valid, lz_rank, lz_lnode, lz_ldest, lz_ctr, lz_table;
   void *h_lz = nullptr;  // pinned mirror of the lazy counters
+  int *h_rflag = nullptr;  // mapped pinned: copy-range flags of DPG_HOST_OUT_PROGRESS
+  int *d_rflag = nullptr;
   int *h_abort = nullptr;             // mapped pinned
   int *d_abort = nullptr;
   // launch choices (dpg_set_tuning): check variant, blocks per SM, the batch
   // size from which the ball scan uses the key grid, pipelined check launches
-  dpg_tuning tune{DPG_CHECK_SLOTS, 0, 2048, 8, 0};
+  dpg_tuning tune{DPG_CHECK_SLOTS, 0, 2048, 8, DPG_HOST_OUT_PROGRESS};
   cudaEvent_t ev[6] = {};
   double timings[4] = {0, 0, 0, 0};
 };

@@ -341,6 +341,7 @@ void dpg_destroy(dpg_ctx *c) {
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
   if (c->h_bases) cudaFreeHost(c->h_bases);
   if (c->h_lz) cudaFreeHost(c->h_lz);
+  if (c->h_rflag) cudaFreeHost(c->h_rflag);
   for (auto &e : c->ev_sub)
     if (e) cudaEventDestroy(e);
   if (c->ev_tot) cudaEventDestroy(c->ev_tot);
@@ -651,7 +652,9 @@ int dpg_set_tuning(dpg_ctx *c, const dpg_tuning *t) {
   if (!c || !t) return DPG_ERR_ARG;
   if ((t->check_variant != DPG_CHECK_LOCKSTEP && t->check_variant != DPG_CHECK_SLOTS) ||
       t->check_blocks_per_sm < 0 || t->check_blocks_per_sm > 32 || t->grid_min_nodes < 0 ||
-      t->pipe_launches < 1 || t->pipe_launches > kMaxSub || (t->direct_host != 0 && t->direct_host != 1))
+      t->pipe_launches < 1 || t->pipe_launches > kMaxSub ||
+      (t->host_output != DPG_HOST_OUT_PIPELINED && t->host_output != DPG_HOST_OUT_DIRECT &&
+       t->host_output != DPG_HOST_OUT_PROGRESS))
     return fail(c, DPG_ERR_ARG, "set_tuning: value out of range");
   c->tune = *t;
   return DPG_OK;
@@ -737,7 +740,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   // cudaHostAlloc, cudaHostRegister): the check kernel writes every result
   // there itself, node ids and primitives included, so no copy follows it
   bool direct = false;
-  if (!dev_out && c->tune.direct_host && !(opts->mode & DPG_MODE_BALL_ONLY) && cap > 0) {
+  if (!dev_out && c->tune.host_output == DPG_HOST_OUT_DIRECT && !(opts->mode & DPG_MODE_BALL_ONLY) && cap > 0) {
     void *hp[7] = {out->node, out->prim, out->verdict, out->first_invalid, out->end_state, out->min_gap, out->flags};
     void *dp[7] = {};
     direct = out->node && out->prim;
@@ -766,6 +769,15 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   // tune.pipe_launches launches over item ranges and each range's results are copied out
   // while the next range is checked
   const bool pipelined = !dev_out && !direct && !(opts->mode & DPG_MODE_BALL_ONLY) && reorder && cap > 0;
+  // one check launch whose warps flag finished copy ranges in mapped memory
+  const bool progress = pipelined && c->tune.host_output == DPG_HOST_OUT_PROGRESS;
+  const int n_ranges = pipelined ? c->tune.pipe_launches : 1;
+  if (progress && !c->h_rflag) {
+    CUDA_TRY(c, cudaHostAlloc(&c->h_rflag, sizeof(int) * kMaxSub, cudaHostAllocMapped));
+    CUDA_TRY(c, cudaHostGetDevicePointer(&c->d_rflag, c->h_rflag, 0));
+  }
+  if (progress)
+    for (int j = 0; j < kMaxSub; j++) reinterpret_cast<volatile int *>(c->h_rflag)[j] = 0;
   if (pipelined) {
     if (!c->cstream) {
       CUDA_TRY(c, cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
@@ -777,6 +789,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     if (c->h_bases_n < (size_t)P + 1) {
       if (c->h_bases) cudaFreeHost(c->h_bases);
   if (c->h_lz) cudaFreeHost(c->h_lz);
+  if (c->h_rflag) cudaFreeHost(c->h_rflag);
       c->h_bases = nullptr;
       c->h_bases_n = 0;
       CUDA_TRY(c, cudaHostAlloc(&c->h_bases, 2 * sizeof(unsigned long long) * (P + 1), cudaHostAllocDefault));
@@ -909,8 +922,10 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       // work-queue counters), so the next range's blocks take the SMs that
       // the previous range's last items leave idle
       ca.perm = reorder ? P_<uint32_t>(c->ord_perm) : nullptr;
-      ca.nsub = pipelined ? c->tune.pipe_launches : 1;
-      pipe_weights(ca.nsub, ca.sub_cum);
+      ca.nsub = pipelined && !progress ? n_ranges : 1;
+      ca.n_ranges = progress ? n_ranges : 0;
+      ca.range_flag = progress ? c->d_rflag : nullptr;
+      pipe_weights(n_ranges, ca.sub_cum);
       for (int j = 0; j < ca.nsub; j++) {
         ca.sub = j;
         cudaStream_t s = pipelined && (j & 1) ? c->xstream : st;
@@ -947,12 +962,20 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
           {out->node, c->p_node.p, 4}, {out->prim, c->p_prim.p, 4}, {out->verdict, c->p_verdict.p, 1},
           {out->first_invalid, c->p_fi.p, 2}, {out->end_state, c->p_end.p, es_bytes * nx},
           {out->min_gap, c->p_gap.p, 4}, {out->flags, c->p_flags.p, 1}};
-      const int np = c->tune.pipe_launches;
+      const int np = n_ranges;
       int cum[kMaxSub + 1];
       pipe_weights(np, cum);
       for (int j = 0; j < np; j++) {
         const int64_t a = pair_at(h0.n_items * cum[j] / cum[np]), e = pair_at(h0.n_items * cum[j + 1] / cum[np]);
-        CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev_sub[j], 0));
+        if (progress) {
+          // the range's flag, or the end of the check (an abort or an error:
+          // the copies below then read final memory and the sync reports it)
+          if (e > a)
+            for (uint64_t it = 0; !reinterpret_cast<volatile int *>(c->h_rflag)[j]; it++)
+              if ((it & 255) == 255 && cudaStreamQuery(st) != cudaErrorNotReady) break;
+        } else {
+          CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev_sub[j], 0));
+        }
         if (e > a)
           for (const auto &f : cp)
             if (f.dst)

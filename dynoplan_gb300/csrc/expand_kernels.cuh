@@ -49,6 +49,7 @@ struct DevCounters {
   unsigned long long n_recheck;
   unsigned long long n_ball_recheck;
   unsigned long long n_overflow;
+  unsigned long long range_done[kMaxSub];  // items finished per copy range (DPG_HOST_OUT_PROGRESS)
   int status;  // 0 ok, DPG_ERR_ABORTED
   unsigned n_bad;  // dpg_check_pairs: pairs whose node or primitive index is out of range
 };

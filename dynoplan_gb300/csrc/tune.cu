@@ -46,7 +46,7 @@ bool cache_lookup(const char *path, const std::string &key, dpg_tuning *t, doubl
   double m = 0;
   bool found = false;
   while (std::fscanf(f, "%255s %d %d %d %d %d %lf", k, &v.check_variant, &v.check_blocks_per_sm,
-                     &v.grid_min_nodes, &v.pipe_launches, &v.direct_host, &m) == 7) {
+                     &v.grid_min_nodes, &v.pipe_launches, &v.host_output, &m) == 7) {
     if (key == k) {  // the last line of a key wins
       *t = v;
       *ms = m;
@@ -62,7 +62,7 @@ void cache_store(const char *path, const std::string &key, const dpg_tuning &t, 
   FILE *f = std::fopen(path, "a");
   if (!f) return;
   std::fprintf(f, "%s %d %d %d %d %d %.6f\n", key.c_str(), t.check_variant, t.check_blocks_per_sm,
-               t.grid_min_nodes, t.pipe_launches, t.direct_host, ms);
+               t.grid_min_nodes, t.pipe_launches, t.host_output, ms);
   std::fclose(f);
 }
 
@@ -132,7 +132,7 @@ extern "C" int dpg_autotune(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, 
     for (int bl : {0, 3, 2})
       for (int g : {2048, INT_MAX}) {
         if (!grid_choice && g != 2048) continue;
-        cand.push_back(dpg_tuning{v, bl, g, r.initial.pipe_launches, r.initial.direct_host});
+        cand.push_back(dpg_tuning{v, bl, g, r.initial.pipe_launches, r.initial.host_output});
       }
   auto time_choice = [&](const dpg_tuning &t, double *ms) -> int {
     int e = dpg_set_tuning(c, &t);

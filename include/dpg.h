@@ -284,12 +284,21 @@ typedef struct dpg_tuning {
   int32_t check_variant;       /* DPG_CHECK_* [DPG_CHECK_SLOTS]; FP64_STRICT always walks lockstep */
   int32_t check_blocks_per_sm; /* resident check blocks per SM, 0 = the occupancy maximum [0] */
   int32_t grid_min_nodes;      /* batches from this size scan the ball through the key grid [2048] */
-  int32_t pipe_launches;       /* check launches of a host-output expand, 1..8 [8] */
-  int32_t direct_host;         /* host outputs in page-locked memory the GPU can map: the check
-                                  kernel writes them itself, no staging copies (1), or the staged,
-                                  pipelined copies (0) [0: on the GB300 hosts measured, the
-                                  kernel's stores over the host link doubled the check time] */
+  int32_t pipe_launches;       /* copy ranges of a host-output expand, 1..8 (check launches with
+                                  DPG_HOST_OUT_PIPELINED) [8] */
+  int32_t host_output;         /* DPG_HOST_OUT_* for host output arrays of a batch >= 2048 nodes
+                                  [DPG_HOST_OUT_PROGRESS] */
 } dpg_tuning;
+/* dpg_tuning.host_output: how results reach host output arrays */
+#define DPG_HOST_OUT_PIPELINED 0 /* pipe_launches check launches over item ranges of decreasing
+                                    size; each range copied (asynchronously when page-locked) once
+                                    its launch is done */
+#define DPG_HOST_OUT_DIRECT 1    /* page-locked arrays the GPU maps: the check kernel writes them
+                                    itself (on the GB300 hosts measured, its stores over the host
+                                    link doubled the check time) */
+#define DPG_HOST_OUT_PROGRESS 2  /* one check launch; its warps count finished items per range
+                                    and the count that completes a range raises a flag in mapped
+                                    host memory, on which the host starts that range's copy */
 int dpg_get_tuning(const dpg_ctx *ctx, dpg_tuning *t);
 int dpg_set_tuning(dpg_ctx *ctx, const dpg_tuning *t);
 

@@ -249,12 +249,13 @@ def test_obstacle_grid_border_cases(gpu, kind, variant):
     compare(kind, res, ora, 0)
 
 
-@pytest.mark.parametrize("cfg,scale,precision", [(2, 0.03, 0), (2, 0.005, 0), (1, 0.3, 1), (3, 0.05, 0)])
+@pytest.mark.parametrize("cfg,scale,precision", [(2, 0.03, 0), (2, 0.005, 0), (1, 0.3, 1), (1, 0.3, 2), (3, 0.05, 0)])
 def test_direct_host_writes(gpu, cfg, scale, precision):
-    """Outputs in page-locked host memory: the check kernel writes them itself
-    (direct_host = 1) -- the same rows as the staged, pipelined copies
-    (direct_host = 0) and the oracle's results; small batches (caller's node
-    order) and spatially ordered ones."""
+    """Outputs in page-locked host memory, by each host-output path: the
+    check kernel writing them itself (DPG_HOST_OUT_DIRECT), one launch with
+    range flags (DPG_HOST_OUT_PROGRESS) and the staged launches
+    (DPG_HOST_OUT_PIPELINED) give the same rows and the oracle's results;
+    small batches (caller's node order) and spatially ordered ones."""
     wl = W.make_workload(cfg, scale=scale, seed=810 + cfg)
     N, nx = wl.nodes.shape
     res = {}
@@ -263,8 +264,8 @@ def test_direct_host_writes(gpu, cfg, scale, precision):
         ctx.upload_env(wl.env)
         n = ctx.expand(wl.nodes, wl.radius, precision=precision)["n_pairs"]
         cap = n + 64
-        for direct in (1, 0):
-            ctx.set_tuning(direct_host=direct)
+        for direct in (1, 2, 0):
+            ctx.set_tuning(host_output=direct)
             pins = {"node": gpu.PinnedArray(cap, np.uint32), "prim": gpu.PinnedArray(cap, np.uint32),
                     "verdict": gpu.PinnedArray(cap, np.uint8), "first_invalid": gpu.PinnedArray(cap, np.int16),
                     "end_state": gpu.PinnedArray((cap, nx), np.float64 if precision else np.float32),
@@ -278,5 +279,6 @@ def test_direct_host_writes(gpu, cfg, scale, precision):
                 v.free()
     for k in ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap", "flags"):
         np.testing.assert_array_equal(res[1][k], res[0][k])
+        np.testing.assert_array_equal(res[2][k], res[0][k])
     ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius, fast=True, threads=ob.lib().orc_max_threads())
     compare(wl.robot.kind, res[1], ora, precision, min_gap=False)
