@@ -66,7 +66,7 @@ CHECK_TRAFFIC_PER_PAIR = {
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=2)
@@ -82,6 +82,8 @@ def parse():
                     help="headline workload only: no expansion arms, no other workloads (profiling runs)")
     ap.add_argument("--nodes", type=int, default=None, help="frontier states per step (default: the workload's)")
     ap.add_argument("--envs", type=int, default=200, help="--config 4: training environments")
+    ap.add_argument("--forward-kernel", type=int, default=2, choices=[0, 1, 2],
+                    help="--config 4: surrogate forward kernel (0 per-layer GEMMs, 1 fused, 2 warp-specialised)")
     ap.add_argument("--problems", type=int, default=100, help="--config 5: evaluation problems")
     ap.add_argument("--train-problems", type=int, default=64, help="--config 5: problems the heuristic learns from")
     return ap.parse_args()
@@ -114,6 +116,12 @@ class Clocks:
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        # the sampler is live (its first row written) before the timed region starts
+        t_end = time.time() + 5
+        while self.p is not None and time.time() < t_end and self.p.poll() is None:
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if self.p is None:
@@ -864,6 +872,7 @@ def run_surrogate(args, rank, world, local_rank):
     held = SG.make_dataset(wl, n_envs=8, nodes_per_env=2000, pairs_per_env=10 ** 6, seed=5, device=dev)
     build_s = time.perf_counter() - t0
     model = SG.Surrogate(wl.prims.P, max_rows=1 << 20, device=dev, seed=0)
+    model.set_fused(args.forward_kernel)
     g = torch.Generator(device=ds.node.device).manual_seed(0)
     n = len(ds)
 
@@ -923,7 +932,7 @@ def run_surrogate(args, rank, world, local_rank):
                      "frac": achieved / peaks["bf16_tflops_sustained"], "traffic": None,
                      "peak_source": f"{src} bf16 sustained",
                      "work_model": "3 x forward FLOPs of the used widths per sample"},
-        "inference": {"pairs": m, "ms": 1e3 * inf_s, "pairs_per_s": m / inf_s,
+        "inference": {"pairs": m, "kernel": args.forward_kernel, "ms": 1e3 * inf_s, "pairs_per_s": m / inf_s,
                       "tflops": mlp_alg_flops(m) / inf_s / 1e12,
                       "frac": mlp_alg_flops(m) / inf_s / 1e12 / peaks["bf16_tflops"]},
         "quality": {"held_out_pairs": m, "collision_rate": float(y.mean()), "precision": precision,

@@ -788,8 +788,6 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     }
     if (c->h_bases_n < (size_t)P + 1) {
       if (c->h_bases) cudaFreeHost(c->h_bases);
-  if (c->h_lz) cudaFreeHost(c->h_lz);
-  if (c->h_rflag) cudaFreeHost(c->h_rflag);
       c->h_bases = nullptr;
       c->h_bases_n = 0;
       CUDA_TRY(c, cudaHostAlloc(&c->h_bases, 2 * sizeof(unsigned long long) * (P + 1), cudaHostAllocDefault));
@@ -853,8 +851,6 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   ca.ctr = ctr;
   ca.abort_flag = c->d_abort;
   ca.band = fp64 ? 0.0 : band;
-  // culling keeps every obstacle within the min_gap cap, the FP64 band and a
-  // slack for the FP32 box arithmetic
   ca.cull_margin = kGapCap + (float)band + 1e-3f;
   ca.dt32 = (float)rp.dt;
   ca.half_len32 = (float)rp.half_len;

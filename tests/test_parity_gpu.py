@@ -5,6 +5,7 @@ states within 1e-9 (DPG_FP64, DPG_FP64_STRICT) or 1e-5 relative (DPG_FP32);
 see tests/parity_util.py.  Precision 0 = DPG_FP32, 1 = DPG_FP64 (FP32 tests
 with FP64 decisions in the bands, FP64 end states), 2 = DPG_FP64_STRICT.
 """
+import dataclasses
 import os
 
 import numpy as np
@@ -282,3 +283,49 @@ def test_direct_host_writes(gpu, cfg, scale, precision):
         np.testing.assert_array_equal(res[2][k], res[0][k])
     ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius, fast=True, threads=ob.lib().orc_max_threads())
     compare(wl.robot.kind, res[1], ora, precision, min_gap=False)
+
+
+def test_context_reuse_growing_set(gpu):
+    """One context through host-buffer expands (the default progress-flag
+    path), lazy checks and a larger re-uploaded motion set gives the rows of
+    fresh contexts; the host staging buffers that grow with the motion set
+    leave the range flags and the lazy counters intact, and a context made
+    after it closes works."""
+    import torch
+    small = W.make_workload(2, scale=0.03, seed=840)
+    big = W.make_workload(2, scale=0.03, seed=841, P=2 * small.prims.P)
+    keys = ("node", "prim", "verdict", "first_invalid", "end_state", "min_gap")
+
+    def lazy(ctx, wl):
+        ball = ctx.expand(wl.nodes, wl.radius, ball_only=True)
+        n = ball["n_pairs"]
+        dev = "cuda:0"
+        x_d = torch.from_numpy(small.nodes).to(dev)
+        node_d = torch.from_numpy(ball["node"].view(np.int32)).to(dev)
+        prim_d = torch.from_numpy(ball["prim"].view(np.int32)).to(dev)
+        outs = {"verdict": torch.empty(n, dtype=torch.uint8, device=dev),
+                "first_invalid": torch.empty(n, dtype=torch.int16, device=dev),
+                "end_state": torch.empty((n, wl.robot.nx), dtype=torch.float32, device=dev),
+                "min_gap": torch.empty(n, dtype=torch.float32, device=dev),
+                "flags": torch.zeros(n, dtype=torch.uint8, device=dev)}
+        torch.cuda.synchronize()
+        st = ctx.lazy_check_device(x_d.data_ptr(), len(small.nodes), n, node_d.data_ptr(), prim_d.data_ptr(),
+                                   {k: v.data_ptr() for k, v in outs.items()}, 8)
+        assert 0 < st["n_accepted"] <= st["n_valid"] <= st["n_checked"] <= n
+
+    with gpu.Context(small.robot) as ctx:
+        assert ctx.tuning()["host_output"] == 2
+        ctx.upload_env(small.env)
+        ctx.upload_primitives(small.prims)
+        r1 = ctx.expand(small.nodes, small.radius)
+        lazy(ctx, small)
+        ctx.upload_primitives(big.prims)
+        r2 = ctx.expand(small.nodes, small.radius)
+        lazy(ctx, small)
+        r3 = ctx.expand(small.nodes, small.radius)
+    f1 = run_gpu(gpu, small, 0)
+    f2 = run_gpu(gpu, dataclasses.replace(small, prims=big.prims), 0)
+    for k in keys:
+        np.testing.assert_array_equal(r1[k], f1[k])
+        np.testing.assert_array_equal(r2[k], f2[k])
+        np.testing.assert_array_equal(r3[k], f2[k])
