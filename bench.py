@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--dropin-nodes", type=int, default=2000, help="nodes of the per-node drop-in arm")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch choices (no autotuner)")
+    ap.add_argument("--min-gap", action="store_true",
+                    help="time the expands with the min_gap output (a clearance diagnostic the reference lacks)")
     ap.add_argument("--tuning", default="", help="launch choices to apply instead of the autotuner, "
                     "e.g. check_variant=0,check_blocks_per_sm=3 (dpg_tuning fields)")
     ap.add_argument("--arm-envs", type=int, default=40, help="training environments of the surrogate arm")
@@ -321,8 +323,8 @@ def run_reference(args, rank, world):
     print(json.dumps(line, default=_np_json), flush=True)
 
 
-def device_outputs(torch, cap, nx, prec, dev):
-    return {
+def device_outputs(torch, cap, nx, prec, dev, min_gap=True):
+    o = {
         "node": torch.empty(cap, dtype=torch.int32, device=dev),
         "prim": torch.empty(cap, dtype=torch.int32, device=dev),
         "verdict": torch.empty(cap, dtype=torch.uint8, device=dev),
@@ -331,19 +333,30 @@ def device_outputs(torch, cap, nx, prec, dev):
         "min_gap": torch.empty(cap, dtype=torch.float32, device=dev),
         "flags": torch.empty(cap, dtype=torch.uint8, device=dev),
     }
+    if not min_gap:
+        del o["min_gap"]
+    return o
 
 
-def measure_device(args, lib, ctx, wl, dev, steps, warmup):
+def outputs_named(min_gap):
+    """the outputs a timed expand produces: the reference's (neighbour pairs,
+    verdict, first invalid state, end state) and the FP64-decision flag;
+    min_gap (a clearance diagnostic the reference does not compute) on request"""
+    return "node, prim, verdict, first_invalid, end_state, flags" + (", min_gap" if min_gap else "")
+
+
+def measure_device(args, lib, ctx, wl, dev, steps, warmup, min_gap=None):
     """Device-resident expand of the workload's nodes: `steps` timed calls
     (CUDA events on the library stream, L2 flushed before each).  Returns
     the timing record and the device output tensors of the last step."""
+    min_gap = args.min_gap if min_gap is None else min_gap
     import torch
     N, nx = wl.nodes.shape
     prec = wl.precision
     n_pairs = ctx.expand(wl.nodes, wl.radius, precision=prec)["n_pairs"]   # sizes the outputs
     cap = int(n_pairs * 1.02) + 1024
     x_d = torch.from_numpy(wl.nodes).to(f"cuda:{dev}")
-    outs = device_outputs(torch, cap, nx, prec, dev)
+    outs = device_outputs(torch, cap, nx, prec, dev, min_gap)
     ptrs = {k: v.data_ptr() for k, v in outs.items()}
     for _ in range(warmup):
         ctx.expand_device(x_d.data_ptr(), N, wl.radius, ptrs, cap, precision=prec)
@@ -429,7 +442,7 @@ def other_workload(args, lib, G, cfg, dev):
         t_e, _ = timed_wall(lib, dev, min(args.steps, 10), lambda: ctx.expand_device(
             m["x_d"].data_ptr(), len(wl.nodes), wl.radius, {k: v.data_ptr() for k, v in m["outs"].items()},
             m["cap"], precision=wl.precision))
-        lazy = LazyArm(lib, ctx, wl, m["x_d"], dev, n, m["cap"], LIMIT_BRANCHING)
+        lazy = LazyArm(lib, ctx, wl, m["x_d"], dev, n, m["cap"], LIMIT_BRANCHING, args.min_gap)
         lz = lazy.measure(min(args.steps, 10), None, eager)
         del lazy
         m.pop("outs")
@@ -437,7 +450,8 @@ def other_workload(args, lib, G, cfg, dev):
     rec = {"workload": wl.name, "robot": wl.robot.name, "dtype": "f64" if wl.precision else "f32",
            "precision": {0: "DPG_FP32", 1: "DPG_FP64 (FP32 tests, FP64 band decisions and end states)"}[wl.precision],
            "primitives": wl.prims.P, "obstacles": len(wl.env.obs_lo), "nodes_per_step": len(wl.nodes),
-           "checked_pairs_per_step": m["n_pairs"], "value": m["pairs_total"] / m["dev_s"], "unit": UNIT,
+           "checked_pairs_per_step": m["n_pairs"], "outputs": outputs_named(args.min_gap),
+           "value": m["pairs_total"] / m["dev_s"], "unit": UNIT,
            "ms_per_step": 1e3 * m["dev_s"] / min(args.steps, 10), "check_ms": 1e3 * m["check_s"],
            "ball_ms": statistics.mean(t[0] for t in m["stage"]),
            "parity": "tests/test_parity_gpu.py::test_full_size_parity (every pair of this workload vs the oracle)",
@@ -524,6 +538,13 @@ def run_ours(args, rank, world, local_rank):
     stage = m["stage"]
     rechecks = m["rechecks"]
     del m
+    # the same expands with the min_gap output as well (not in the timed value above)
+    with_mg = None
+    if not args.min_gap:
+        m2 = measure_device(args, lib, ctx, wl, dev, min(args.steps, 20), args.warmup, min_gap=True)
+        with_mg = {"outputs": outputs_named(True), "value": m2["pairs_total"] / m2["dev_s"],
+                   "ms_per_step": 1e3 * m2["dev_s"] / min(args.steps, 20), "check_ms": 1e3 * m2["check_s"]}
+        del m2
 
     # ---------------- e2e through the C ABI with host buffers
     e2e, pinned = None, []
@@ -564,8 +585,10 @@ def run_ours(args, rank, world, local_rank):
                    "nodes_per_step": N, "delta": wl.delta, "alpha": wl.alpha, "radius": wl.radius,
                    "checked_pairs_per_step": n_pairs, "fp64_rechecks_per_step": rechecks // args.steps,
                    "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",
-                   "parallelism": f"replicas x{world}", "wall_ms_per_step": 1e3 * wall / args.steps},
+                   "parallelism": f"replicas x{world}", "wall_ms_per_step": 1e3 * wall / args.steps,
+                   "outputs": outputs_named(args.min_gap)},
         "e2e": e2e,
+        **({"with_min_gap": with_mg} if with_mg else {}),
         **({"variant_radius_delta": variant} if variant else {}),
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "roofline": roof,
@@ -601,7 +624,7 @@ class LazyArm:
     """ball-only dpg_expand + (scores) + dpg_lazy_check on the workload's
     nodes, with device buffers for n_cand candidates"""
 
-    def __init__(self, lib, ctx, wl, x_d, dev, n_cand, cap, limit):
+    def __init__(self, lib, ctx, wl, x_d, dev, n_cand, cap, limit, min_gap=False):
         import torch
         nx = wl.nodes.shape[1]
         self.lib, self.ctx, self.wl, self.x_d, self.dev = lib, ctx, wl, x_d, dev
@@ -613,8 +636,9 @@ class LazyArm:
         self.lz = {"verdict": torch.empty(cap, dtype=torch.uint8, device=dev),
                    "first_invalid": torch.empty(cap, dtype=torch.int16, device=dev),
                    "end_state": torch.empty((cap, nx), dtype=es_t, device=dev),
-                   "min_gap": torch.empty(cap, dtype=torch.float32, device=dev),
                    "flags": torch.empty(cap, dtype=torch.uint8, device=dev)}
+        if min_gap:
+            self.lz["min_gap"] = torch.empty(cap, dtype=torch.float32, device=dev)
         self.lptr = {k: v.data_ptr() for k, v in self.lz.items()}
 
     def run(self, score_fn=None):
@@ -704,7 +728,7 @@ def run_arms(args, lib, G, ctx, wl, x_d, dev):
     # ---- candidates (ball only) and the batched eager expand
     n_cand = ctx.expand(wl.nodes, wl.radius, precision=0, ball_only=True)["n_pairs"]
     cap = n_cand + 1024
-    eag = device_outputs(torch, cap, nx, 0, dev)
+    eag = device_outputs(torch, cap, nx, 0, dev, args.min_gap)
     eptr = {k: v.data_ptr() for k, v in eag.items()}
 
     t_b, _ = timed_wall(lib, dev, steps, lambda: ctx.expand_device(x_d.data_ptr(), N, wl.radius, eptr, cap,
@@ -715,7 +739,7 @@ def run_arms(args, lib, G, ctx, wl, x_d, dev):
     prim_h = eag["prim"][:n_cand].cpu().numpy().view(np.uint32)
 
     # ---- lazy arms: candidates, (scores), lazy check
-    lazy = LazyArm(lib, ctx, wl, x_d, dev, n_cand, cap, limit)
+    lazy = LazyArm(lib, ctx, wl, x_d, dev, n_cand, cap, limit, args.min_gap)
 
     out["batched_lazy"] = lazy.measure(steps, None, (node_h, prim_h, v_eager))
 
@@ -762,9 +786,10 @@ def run_radius_variant(args, lib, ctx, wl, x_d, prec, dev):
         "verdict": torch.empty(cap, dtype=torch.uint8, device=dev),
         "first_invalid": torch.empty(cap, dtype=torch.int16, device=dev),
         "end_state": torch.empty((cap, nx), dtype=torch.float64 if prec != 0 else torch.float32, device=dev),
-        "min_gap": torch.empty(cap, dtype=torch.float32, device=dev),
         "flags": torch.empty(cap, dtype=torch.uint8, device=dev),
     }
+    if args.min_gap:
+        outs["min_gap"] = torch.empty(cap, dtype=torch.float32, device=dev)
     ptrs = {k: v.data_ptr() for k, v in outs.items()}
     for _ in range(args.warmup):
         ctx.expand_device(x_d.data_ptr(), N, radius, ptrs, cap, precision=prec)
@@ -788,8 +813,10 @@ def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
         "node": G.PinnedArray(cap, np.uint32), "prim": G.PinnedArray(cap, np.uint32),
         "verdict": G.PinnedArray(cap, np.uint8), "first_invalid": G.PinnedArray(cap, np.int16),
         "end_state": G.PinnedArray((cap, nx), np.float64 if prec != 0 else np.float32),
-        "min_gap": G.PinnedArray(cap, np.float32), "flags": G.PinnedArray(cap, np.uint8),
+        "flags": G.PinnedArray(cap, np.uint8),
     }
+    if args.min_gap:
+        hosts["min_gap"] = G.PinnedArray(cap, np.float32)
     host_out = {k: v.array for k, v in hosts.items()}
     for _ in range(args.warmup):
         ctx.expand(xh.array, wl.radius, precision=prec, capacity=cap, outputs=host_out)
@@ -800,7 +827,7 @@ def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
         r = ctx.expand(xh.array, wl.radius, precision=prec, capacity=cap, outputs=host_out)
         e2e_s += time.perf_counter() - t0
         e2e_pairs += r["n_pairs"]
-    d2h = n_pairs * (4 + 4 + 1 + 2 + es_bytes * nx + 4 + 1)
+    d2h = n_pairs * (4 + 4 + 1 + 2 + es_bytes * nx + 1 + (4 if args.min_gap else 0))
     e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * nx * 8),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s / args.steps}
     return e2e, list(hosts.values()) + [xh]

@@ -105,7 +105,7 @@ extern "C" int dpg_bench_per_node_expand(dpg_ctx *ctx, const dpg_expand_opts *op
       out.verdict = (uint8_t *)buf[2];
       out.first_invalid = (int16_t *)buf[3];
       out.end_state = buf[4];
-      out.min_gap = (float *)buf[5];
+      out.min_gap = nullptr;  // the reference's outputs: no clearance diagnostic
       out.flags = (uint8_t *)buf[6];
       rc = dpg_expand(ctx, &o, 1, x + i * nx, &out);
       if (rc == DPG_ERR_CAPACITY) {

@@ -16,8 +16,8 @@
 // or velocity); the canonical rollout is FP64, once per upload.
 //
 // Obstacles (shared memory) are culled per lane in two levels, both with a
-// margin of kGapCap + band + slack so nothing that could touch the robot,
-// fall in the FP64 band or set min_gap is dropped:
+// margin of band + slack (+ kGapCap when min_gap is an output) so nothing that
+// could touch the robot, fall in the FP64 band or set min_gap is dropped:
 //   1. against the bounding box of the whole transformed primitive (once per
 //      pair; bitmask over <= kMaxCullObs obstacles),
 //   2. against the box of each chunk of R::CHUNK states (from the level-1 set),
@@ -68,6 +68,11 @@ struct CheckArgs {
   // slot variant: byte offset of the per-warp scratch in dynamic shared memory
   int slot_offset;
 };
+
+// Obstacle culling margin: every obstacle within the FP64 band, plus a slack
+// for the FP32 box arithmetic, and within the min_gap cap when min_gap is an
+// output (without it, obstacles farther than the band change no result).
+inline float cull_margin(bool min_gap, double band) { return (min_gap ? kGapCap : 0.f) + (float)band + 1e-3f; }
 
 template <class Real> __device__ __forceinline__ const Pose<Real> *pose_table(const PrimView &pv);
 template <> __device__ __forceinline__ const Pose<float> *pose_table<float>(const PrimView &pv) { return pv.pose32; }
@@ -469,22 +474,31 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
 //
 // The lockstep walk above makes every state cost the largest candidate count
 // of any lane: lanes with fewer candidates (most have none) wait.  This
-// variant keeps the walk over chunks of R::CHUNK states but runs each
-// chunk's narrow phase as a list of (lane, candidate obstacle) slots spread
-// over the warp's 32 lanes; a slot tests its obstacle against every state of
-// the chunk (all parts) and stops at its first contact.  Per lane and state,
-// the contacts, the FP64 decisions and the minimum axis-aligned gap are merged
-// in shared memory; each lane then folds the states up to its first contact,
-// which gives exactly the per-state results of the sequential walk (every
-// candidate is tested at every state up to the first contact).  FP32 tests
-// with FP64 decisions in the band; the bounds tests stay per lane.
+// variant keeps the walk over chunks of R::CHUNK states but runs the narrow
+// phase as a list of (lane, chunk, candidate obstacle) slots spread over the
+// warp's 32 lanes; a slot tests its obstacle against every state of its chunk
+// (all parts) and stops at its first contact.  One narrow round takes
+// consecutive chunks until the warp has about a round of slots (car1 chunks
+// average about 10 slots a warp), at most 32 states; chunks after a lane's
+// first contact are tested speculatively and discarded by the fold.  Per lane
+// and state, the contacts, the FP64 decisions and the minimum axis-aligned gap
+// are merged in shared memory; each lane then folds the states up to its first
+// contact, which gives exactly the per-state results of the sequential walk
+// (every candidate is tested at every state up to the first contact).  FP32
+// tests with FP64 decisions in the band; the bounds tests stay per lane.
 
-template <int CH, int PARTS> struct SlotScratch {
-  Pose<float> pose[CH * PARTS];  // the chunk's pose rows, [j * PARTS + q]
-  float4 aabb[CH * PARTS];       // planar robots: (centre x, centre y, half x, half y) of each part
-  unsigned mg[CH][32];           // per state and lane: min axis-aligned gap (order-preserving bits)
-  unsigned hit[32];              // per lane: bit j = contact at state k0 + j
-  unsigned rc[32];               // per lane: bit j = a test at k0 + j was decided in FP64
+constexpr int kSlotFill = 24;  // a narrow round stops taking chunks at this many slots
+
+template <int CH, int PARTS, int NW> struct SlotScratch {
+  static constexpr int GMAX = 32 / CH;  // chunks a round can take (32 hit bits)
+  static constexpr int MGS = 16;        // states a round takes when min_gap is an output
+  Pose<float> pose[32 * PARTS];         // the round's pose rows, [s * PARTS + q]
+  float2 ext[32 * PARTS];               // planar robots: axis-aligned half extents of each part
+  unsigned cm[GMAX][NW][32];            // per chunk, word and lane: the chunk's candidates
+  unsigned l1[NW][32];                  // per word and lane: level-1 candidates
+  unsigned mg[MGS][32];                 // per state and lane: min axis-aligned gap (order-preserving bits)
+  unsigned hit[32];                     // per lane: bit s = contact at state k0 + s
+  unsigned rc[32];                      // per lane: bit s = a test at k0 + s was decided in FP64
 };
 
 __device__ __forceinline__ unsigned ord_gap(float f) {
@@ -495,18 +509,20 @@ __device__ __forceinline__ float unord_gap(unsigned u) {
   return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
-template <int KIND>
+template <int KIND, int NW>
 constexpr size_t slot_scratch_bytes() {
-  return sizeof(SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS>);
+  return sizeof(SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS, NW>);
 }
 
 template <int KIND, int NW, bool ES64>
 __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
-                                SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS> &S, int p, int64_t pair,
+                                SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS, NW> &S, int p, int64_t pair,
                                 uint32_t node, bool active) {
   using R = Robot<KIND>;
+  using Scratch = SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS, NW>;
   constexpr int D = R::POSD, V = R::VELOFF, CH = R::CHUNK, PARTS = R::PARTS;
   static_assert(NW > 0, "the slot variant needs the candidate bitmasks");
+  static_assert(CH <= 16 && Scratch::MGS % CH == 0, "5-bit state counts; whole chunks under the min_gap limit");
   const int lane = threadIdx.x & 31;
   const PrimView &pv = A.pv;
   const RobotParams &rp = A.rp;
@@ -516,6 +532,8 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
   const float band = A.band32, dt = A.dt32;
   const double *x64 = A.nv.x64 + (int64_t)(active ? node : 0) * R::NX;
   const int n_obs = A.ev.n_obs;
+  const bool want_mg = A.out.min_gap != nullptr;  // per-state gap merges only for that output
+  const int GL = want_mg ? Scratch::MGS / CH : Scratch::GMAX;
 
   float off[D + V];
 #pragma unroll
@@ -543,9 +561,8 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
   }
 
   // level-1 culling against the whole transformed primitive
-  uint32_t l1[NW] = {};
   const float M = A.cull_margin;
-  if (active) {
+  {
     const float *tb = pv.tbox32 + (int64_t)p * 2 * D;
     const float tmax = float(L - 1) * dt;
     float cen[D], hf[D];
@@ -562,10 +579,12 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
 #pragma unroll
     for (int w = 0; w < NW; w++) {
       uint32_t bits = 0u;
-      const int o0 = 32 * w, o1 = min(n_obs, o0 + 32);
-      for (int o = o0; o < o1; o++)
-        if (near_box<D, float>(cen, hf, obs_sm, o, M)) bits |= 1u << (o - o0);
-      l1[w] = bits;
+      if (active) {
+        const int o0 = 32 * w, o1 = min(n_obs, o0 + 32);
+        for (int o = o0; o < o1; o++)
+          if (near_box<D, float>(cen, hf, obs_sm, o, M)) bits |= 1u << (o - o0);
+      }
+      S.l1[w][lane] = bits;
     }
   }
 
@@ -574,101 +593,111 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
   float mg = INFINITY;
   const float hl = A.half_len32, hw = A.half_wid32, rad = A.radius32;
 
-  for (int k0 = 0; k0 < L; k0 += CH) {
+  for (int k0 = 0; k0 < L;) {
     if (!__any_sync(kFull, !done)) break;
-    const int kend = min(L, k0 + CH);
-    // the chunk's box: level-2 culling and whether its states need bounds tests
-    uint32_t cm[NW];
-#pragma unroll
-    for (int w = 0; w < NW; w++) cm[w] = 0u;
-    bool nb = false;
-    if (!done) {
-      const float *cb = pv.cbox32 + (pv.coff[p] + k0 / CH) * 2 * D;
-      const float t0 = float(k0) * dt, t1 = float(kend - 1) * dt;
-      float cen[D], hf[D];
-#pragma unroll
-      for (int i = 0; i < D; i++) {
-        cen[i] = cb[i] + off[i];
-        hf[i] = cb[D + i];
-        if (V) {
-          const float v = off[D + i];
-          cen[i] += 0.5f * (t0 + t1) * v;
-          hf[i] += 0.5f * (t1 - t0) * fabsf(v);
-        }
-      }
-      if (!collided) {
-#pragma unroll
-        for (int w = 0; w < NW; w++) {
-          uint32_t m = l1[w], c = 0;
-          while (m) {
-            const int b = __ffs(m) - 1;
-            m &= m - 1;
-            if (near_box<D, float>(cen, hf, obs_sm, 32 * w + b, M)) c |= 1u << b;
-          }
-          cm[w] = c;
-        }
-      }
-      if (need_bounds) {
-        bool in = true;
-#pragma unroll
-        for (int i = 0; i < D; i++)
-          in = in && cen[i] - hf[i] > A.lo32[i] + band + 1e-3f && cen[i] + hf[i] < A.hi32[i] - band - 1e-3f;
-        nb = !in;
-      }
-    }
-    // bounds tests of the chunk's states, per lane, up to the first state out
-    int j_oob = CH;
-    if (nb) {
-      for (int k = k0; k < kend; k++) {
-        const Pose<float> ps = pose[s0 + k];  // part 0 = the state position
-        const float t = float(k) * dt;
-        const float pv3[3] = {ps.cx + off[0] + (V ? t * off[D] : 0.f), ps.cy + off[1] + (V ? t * off[D + 1] : 0.f),
-                              D == 3 ? ps.c + off[2] + (V ? t * off[D + 2] : 0.f) : 0.f};
-        int bt = 0;
+    // the round's chunks: level-2 culling, bounds tests, per-chunk state and candidate counts
+    uint32_t nsts = 0u, ncs = 0u;  // chunk g: states to test (5 bits at 5g), candidates (8 bits at 8g)
+    int n_lane = 0;                // this lane's slots in the round
+    int G = 0, kk = k0;
+    while (true) {
+      const int kend = min(L, kk + CH);
+      int nc = 0;
+      bool nb = false;
+      if (!done) {
+        const float *cb = pv.cbox32 + (pv.coff[p] + kk / CH) * 2 * D;
+        const float t0 = float(kk) * dt, t1 = float(kend - 1) * dt;
+        float cen[D], hf[D];
 #pragma unroll
         for (int i = 0; i < D; i++) {
-          const float v = pv3[i], lo = A.lo32[i], hi = A.hi32[i];
-          int r = (v < lo - band || v > hi + band) ? 1 : ((v <= lo + band || v >= hi - band) ? 2 : 0);
-          if (r == 2) {  // decide in FP64
-            const double v64 = pos64<KIND>(A, s0 + k, k, x64, i);
-            r = (v64 >= A.ev.lo[i] && v64 <= A.ev.hi[i]) ? 0 : 1;
-            rechecked = true;
+          cen[i] = cb[i] + off[i];
+          hf[i] = cb[D + i];
+          if (V) {
+            const float v = off[D + i];
+            cen[i] += 0.5f * (t0 + t1) * v;
+            hf[i] += 0.5f * (t1 - t0) * fabsf(v);
           }
-          bt |= r;
         }
-        if (bt) {
-          j_oob = k - k0;
-          break;
+        if (!collided) {
+#pragma unroll
+          for (int w = 0; w < NW; w++) {
+            uint32_t m = S.l1[w][lane], c = 0;
+            while (m) {
+              const int b = __ffs(m) - 1;
+              m &= m - 1;
+              if (near_box<D, float>(cen, hf, obs_sm, 32 * w + b, M)) c |= 1u << b;
+            }
+            S.cm[G][w][lane] = c;
+            nc += __popc(c);
+          }
+        }
+        if (need_bounds) {
+          bool in = true;
+#pragma unroll
+          for (int i = 0; i < D; i++)
+            in = in && cen[i] - hf[i] > A.lo32[i] + band + 1e-3f && cen[i] + hf[i] < A.hi32[i] - band - 1e-3f;
+          nb = !in;
         }
       }
-    }
-    // the narrow phase as (lane, candidate) slots
-    const int nst = (!done && !collided) ? min(kend - k0, j_oob) : 0;
-    int nc = 0;
-    if (nst > 0) {
+      // bounds tests of the chunk's states, per lane, up to the first state out
+      int j_oob = CH;
+      if (nb) {
+        for (int k = kk; k < kend; k++) {
+          const Pose<float> ps = pose[s0 + k];  // part 0 = the state position
+          const float t = float(k) * dt;
+          const float pv3[3] = {ps.cx + off[0] + (V ? t * off[D] : 0.f), ps.cy + off[1] + (V ? t * off[D + 1] : 0.f),
+                                D == 3 ? ps.c + off[2] + (V ? t * off[D + 2] : 0.f) : 0.f};
+          int bt = 0;
 #pragma unroll
-      for (int w = 0; w < NW; w++) nc += __popc(cm[w]);
+          for (int i = 0; i < D; i++) {
+            const float v = pv3[i], lo = A.lo32[i], hi = A.hi32[i];
+            int r = (v < lo - band || v > hi + band) ? 1 : ((v <= lo + band || v >= hi - band) ? 2 : 0);
+            if (r == 2) {  // decide in FP64
+              const double v64 = pos64<KIND>(A, s0 + k, k, x64, i);
+              r = (v64 >= A.ev.lo[i] && v64 <= A.ev.hi[i]) ? 0 : 1;
+              rechecked = true;
+            }
+            bt |= r;
+          }
+          if (bt) {
+            j_oob = k - kk;
+            break;
+          }
+        }
+      }
+      const int nst = (!done && !collided) ? min(kend - kk, j_oob) : 0;
+      if (nst == 0) nc = 0;
+      nsts |= (uint32_t)nst << (5 * G);
+      ncs |= (uint32_t)nc << (8 * G);
+      n_lane += nc;
+      if (!done && j_oob < CH) {  // later states of this lane are never tested
+        first_oob = kk + j_oob;
+        done = true;
+      }
+      G++;
+      kk = kend;
+      if (G >= GL || kk >= L) break;
+      if (__reduce_add_sync(kFull, (unsigned)n_lane) >= (unsigned)kSlotFill) break;
     }
-    int pre = nc;
+    const int nS = kk - k0;  // states of the round, <= 32 (<= MGS with min_gap)
+    // the narrow phase as (lane, chunk, candidate) slots
+    int pre = n_lane;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const int v = __shfl_up_sync(kFull, pre, d);
       if (lane >= d) pre += v;
     }
     const int T = __shfl_sync(kFull, pre, 31);
-    pre -= nc;  // exclusive prefix
+    pre -= n_lane;  // exclusive prefix
     if (T > 0) {
-      if (lane < CH * PARTS) {
-        const int j = lane / PARTS, q = lane % PARTS;
-        if (k0 + j < L) {
-          const Pose<float> ps = pose[(int64_t)q * pv.S + s0 + k0 + j];
-          S.pose[lane] = ps;
-          const float ac = fabsf(ps.c), as = fabsf(ps.s);
-          S.aabb[lane] = make_float4(ps.cx, ps.cy, hl * ac + hw * as, hl * as + hw * ac);
-        }
+      for (int e = lane; e < nS * PARTS; e += 32) {
+        const int j = e / PARTS, q = e % PARTS;
+        const Pose<float> ps = pose[(int64_t)q * pv.S + s0 + k0 + j];
+        S.pose[e] = ps;
+        const float ac = fabsf(ps.c), as = fabsf(ps.s);
+        S.ext[e] = make_float2(hl * ac + hw * as, hl * as + hw * ac);
       }
-#pragma unroll
-      for (int j = 0; j < CH; j++) S.mg[j][lane] = ord_gap(INFINITY);
+      if (want_mg)
+        for (int j = 0; j < nS; j++) S.mg[j][lane] = ord_gap(INFINITY);
       S.hit[lane] = 0u;
       S.rc[lane] = 0u;
       __syncwarp();
@@ -682,21 +711,28 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
           if (cand < 32 && pv_ <= t) owner = cand;
         }
         const int opre = __shfl_sync(kFull, pre, owner);
-        const int onst = __shfl_sync(kFull, nst, owner);
+        const uint32_t onsts = __shfl_sync(kFull, nsts, owner);
+        const uint32_t oncs = __shfl_sync(kFull, ncs, owner);
         const uint32_t onode = __shfl_sync(kFull, node, owner);
-        uint32_t ocm[NW];
-#pragma unroll
-        for (int w = 0; w < NW; w++) ocm[w] = __shfl_sync(kFull, cm[w], owner);
         float osh[D + V];
 #pragma unroll
         for (int i = 0; i < D + V; i++) osh[i] = __shfl_sync(kFull, off[i], owner);
         if (t < T) {
-          int cidx = t - opre, o = -1;
+          // the slot's chunk g and candidate index within it
+          int cidx = t - opre, g = 0;
+          for (; g < Scratch::GMAX - 1; g++) {
+            const int c = (oncs >> (8 * g)) & 255u;
+            if (cidx < c) break;
+            cidx -= c;
+          }
+          const int onst = (onsts >> (5 * g)) & 31u;
+          int o = -1;
 #pragma unroll
           for (int w = 0; w < NW; w++) {
-            const int c = __popc(ocm[w]);
             if (o < 0) {
-              if (cidx < c) o = 32 * w + (int)__fns(ocm[w], 0u, cidx + 1);
+              const uint32_t ow = S.cm[g][w][owner];
+              const int c = __popc(ow);
+              if (cidx < c) o = 32 * w + (int)__fns(ow, 0u, cidx + 1);
               else cidx -= c;
             }
           }
@@ -704,8 +740,9 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
             const double *ox64 = A.nv.x64 + (int64_t)onode * R::NX;
             using Ob = std::conditional_t<R::SPHERE, Obs3<float>, Obs2<float>>;
             const Ob ob = ((const Ob *)obs_sm)[o];
+            const int sb = g * CH;  // the chunk's first state in the round
             for (int j = 0; j < onst; j++) {
-              const int k = k0 + j;
+              const int sj = sb + j, k = k0 + sj;
               float sx = osh[0], sy = osh[1], sz = 0.f;
               if (V) {
                 const float tk = float(k) * dt;
@@ -715,39 +752,38 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
               } else if (D == 3) {
                 sz = osh[2];
               }
-              float g = INFINITY;
+              float gmin = INFINITY;
               bool hit = false;
 #pragma unroll
               for (int q = 0; q < PARTS; q++) {
                 int r;
+                const Pose<float> ps = S.pose[sj * PARTS + q];
                 if constexpr (R::SPHERE) {
-                  const Pose<float> ps = S.pose[j * PARTS + q];
-                  r = sphere_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c + sz, ob, rad, band, g);
+                  r = sphere_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c + sz, ob, rad, band, gmin);
                 } else {
                   // axis-aligned reject first; the oriented axes only within the band
-                  const float4 bb = S.aabb[j * PARTS + q];
-                  const float dx = bb.x + sx - ob.cx, dy = bb.y + sy - ob.cy;
-                  const float ga = fmaxf(fabsf(dx) - (bb.z + ob.hx), fabsf(dy) - (bb.w + ob.hy));
-                  g = fminf(g, ga);
+                  const float2 ex = S.ext[sj * PARTS + q];
+                  const float dx = ps.cx + sx - ob.cx, dy = ps.cy + sy - ob.cy;
+                  const float ga = fmaxf(fabsf(dx) - (ex.x + ob.hx), fabsf(dy) - (ex.y + ob.hy));
+                  gmin = fminf(gmin, ga);
                   if (ga > band) {
                     r = 0;
                   } else {
-                    const Pose<float> ps = S.pose[j * PARTS + q];
                     float unused = INFINITY;
-                    r = planar_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c, ps.s, bb.z, bb.w, ob, hl, hw, band,
+                    r = planar_test<float, true>(ps.cx + sx, ps.cy + sy, ps.c, ps.s, ex.x, ex.y, ob, hl, hw, band,
                                                  unused);
                   }
                 }
                 if (r == 2) {  // decide in FP64
                   r = gap64<KIND>(A, s0, k, q, ox64, o) <= 0.0 ? 1 : 0;
-                  atomicOr(&S.rc[owner], 1u << j);
+                  atomicOr(&S.rc[owner], 1u << sj);
                 }
                 hit |= r == 1;
               }
               // gaps above the cap are reported as +inf: only smaller ones are merged
-              if (g <= kGapCap) atomicMin(&S.mg[j][owner], ord_gap(g));
+              if (want_mg && gmin <= kGapCap) atomicMin(&S.mg[sj][owner], ord_gap(gmin));
               if (hit) {
-                atomicOr(&S.hit[owner], 1u << j);
+                atomicOr(&S.hit[owner], 1u << sj);
                 break;  // later states of this candidate lie past the lane's first contact
               }
             }
@@ -755,26 +791,21 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
         }
       }
       __syncwarp();
-      if (nst > 0) {
+      if (n_lane > 0) {
         const unsigned h = S.hit[lane];
-        const int last = h ? __ffs(h) - 1 : nst - 1;
-        for (int j = 0; j <= last; j++) mg = fminf(mg, unord_gap(S.mg[j][lane]));
+        const int last = h ? __ffs(h) - 1 : nS - 1;
+        if (want_mg)
+          for (int j = 0; j <= last; j++) mg = fminf(mg, unord_gap(S.mg[j][lane]));
         if (S.rc[lane] & (last >= 31 ? 0xffffffffu : ((2u << last) - 1u))) rechecked = true;
         if (h) {
           collided = true;
           first_col = k0 + last;
         }
       }
-      __syncwarp();  // the next chunk reuses the scratch
+      __syncwarp();  // the next round reuses the scratch
     }
-    if (!done) {
-      if (j_oob < CH) {
-        first_oob = k0 + j_oob;
-        done = true;
-      } else if (collided && !need_bounds) {
-        done = true;
-      }
-    }
+    if (!done && collided && !need_bounds) done = true;
+    k0 = kk;
   }
 
   const unsigned rmask = __ballot_sync(kFull, active && rechecked);
@@ -920,7 +951,7 @@ __global__ void __launch_bounds__(kCheckThreads, SLOTS ? Robot<KIND>::SLOT_BLOCK
     const bool active = pair < end;
     const uint32_t node = active ? A.out.node[pair] : 0u;
     if constexpr (SLOTS) {
-      using Scratch = SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS>;
+      using Scratch = SlotScratch<Robot<KIND>::CHUNK, Robot<KIND>::PARTS, NW>;
       Scratch *scr = reinterpret_cast<Scratch *>(smem + A.slot_offset) + (threadIdx.x >> 5);
       check_one_slots<KIND, NW, ES64>(A, smem, *scr, p, (int64_t)pair, node, active);
     } else {

@@ -129,10 +129,10 @@ static void launch_check(dpg_ctx *c, const CheckArgs &ca, int prec, cudaStream_t
   const size_t sm_obs = (ob * std::max(c->n_obs, 1) + 15) / 16 * 16;
   // the slot-parallel narrow phase for FP32 tests with culling
   const bool slots = !fp64 && nw > 0 && c->tune.check_variant == DPG_CHECK_SLOTS;
-  const size_t sm = sm_obs + (slots ? slot_scratch_bytes<KIND>() * (kCheckThreads / 32) : 0);
   CheckArgs a = ca;
   a.slot_offset = (int)sm_obs;
-  auto go = [&](auto kern) {
+  auto go = [&](auto kern, size_t scratch = 0) {
+    const size_t sm = sm_obs + scratch * (kCheckThreads / 32);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCheckThreads, sm);
@@ -144,10 +144,10 @@ static void launch_check(dpg_ctx *c, const CheckArgs &ca, int prec, cudaStream_t
     constexpr bool BAND = decltype(band)::value, ES64 = decltype(es64)::value;
     constexpr bool F32 = sizeof(Real) == 4;
     switch (nw) {
-      case 1: slots ? go(check_pairs<KIND, Real, BAND, 1, ES64, F32>) : go(check_pairs<KIND, Real, BAND, 1, ES64>); break;
-      case 2: slots ? go(check_pairs<KIND, Real, BAND, 2, ES64, F32>) : go(check_pairs<KIND, Real, BAND, 2, ES64>); break;
-      case 3: slots ? go(check_pairs<KIND, Real, BAND, 3, ES64, F32>) : go(check_pairs<KIND, Real, BAND, 3, ES64>); break;
-      case 4: slots ? go(check_pairs<KIND, Real, BAND, 4, ES64, F32>) : go(check_pairs<KIND, Real, BAND, 4, ES64>); break;
+      case 1: slots ? go(check_pairs<KIND, Real, BAND, 1, ES64, F32>, slot_scratch_bytes<KIND, 1>()) : go(check_pairs<KIND, Real, BAND, 1, ES64>); break;
+      case 2: slots ? go(check_pairs<KIND, Real, BAND, 2, ES64, F32>, slot_scratch_bytes<KIND, 2>()) : go(check_pairs<KIND, Real, BAND, 2, ES64>); break;
+      case 3: slots ? go(check_pairs<KIND, Real, BAND, 3, ES64, F32>, slot_scratch_bytes<KIND, 3>()) : go(check_pairs<KIND, Real, BAND, 3, ES64>); break;
+      case 4: slots ? go(check_pairs<KIND, Real, BAND, 4, ES64, F32>, slot_scratch_bytes<KIND, 4>()) : go(check_pairs<KIND, Real, BAND, 4, ES64>); break;
       default: go(check_pairs<KIND, Real, BAND, 0, ES64>); break;
     }
   };
@@ -851,7 +851,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   ca.ctr = ctr;
   ca.abort_flag = c->d_abort;
   ca.band = fp64 ? 0.0 : band;
-  ca.cull_margin = kGapCap + (float)band + 1e-3f;
+  ca.cull_margin = cull_margin(pv_out.min_gap != nullptr, band);
   ca.dt32 = (float)rp.dt;
   ca.half_len32 = (float)rp.half_len;
   ca.half_wid32 = (float)rp.half_wid;
@@ -1171,7 +1171,7 @@ int dpg_expand_noalloc(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const
   ca.ctr = ctr;
   ca.abort_flag = c->d_abort;
   ca.band = fp64 ? 0.0 : band;
-  ca.cull_margin = kGapCap + (float)band + 1e-3f;
+  ca.cull_margin = cull_margin(po.min_gap != nullptr, band);
   ca.dt32 = (float)rp.dt;
   ca.half_len32 = (float)rp.half_len;
   ca.half_wid32 = (float)rp.half_wid;
@@ -1295,7 +1295,7 @@ CheckArgs ctx_check_args(dpg_ctx *c, int prec, double contact_band, const NodeVi
   ca.ctr = c->d_ctr;
   ca.abort_flag = c->d_abort;
   ca.band = prec == DPG_FP64_STRICT ? 0.0 : band;
-  ca.cull_margin = kGapCap + (float)band + 1e-3f;
+  ca.cull_margin = cull_margin(out.min_gap != nullptr, band);
   ca.dt32 = (float)rp.dt;
   ca.half_len32 = (float)rp.half_len;
   ca.half_wid32 = (float)rp.half_wid;

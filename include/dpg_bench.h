@@ -28,7 +28,9 @@ int dpg_bench_flush_l2(int device, size_t bytes);
  * when expand_lazy + check_lazy_trajectory (src/dbastar/dbastar.cpp:806-818)
  * call the GPU for each node it pops (the reference checks the ball
  * lazily; the drop-in checks it in one call).  x: n_nodes x nx host doubles.
- * Writes the checked pairs and the wall time in seconds. */
+ * Outputs per call: node, prim, verdict, first_invalid, end_state, flags
+ * (host buffers; no min_gap).  Writes the checked pairs and the wall time in
+ * seconds. */
 int dpg_bench_per_node_expand(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t n_nodes, int32_t nx,
                               const double *x, int64_t *pairs, double *seconds);
 

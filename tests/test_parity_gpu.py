@@ -329,3 +329,27 @@ def test_context_reuse_growing_set(gpu):
         np.testing.assert_array_equal(r1[k], f1[k])
         np.testing.assert_array_equal(r2[k], f2[k])
         np.testing.assert_array_equal(r3[k], f2[k])
+
+
+@pytest.mark.parametrize("cfg,scale,precision", [(1, 0.3, 1), (2, 0.03, 0), (2, 0.03, 1), (3, 0.01, 0), (5, 0.01, 0)])
+def test_min_gap_optional(gpu, cfg, scale, precision):
+    """Without the min_gap output the check culls obstacles with the FP64 band
+    alone and skips the per-state gap merges: every other output is the same
+    as with it, and the oracle's."""
+    wl = W.make_workload(cfg, scale=scale, seed=860 + cfg)
+    nx = wl.nodes.shape[1]
+    with gpu.Context(wl.robot) as ctx:
+        ctx.upload_primitives(wl.prims)
+        ctx.upload_env(wl.env)
+        full = ctx.expand(wl.nodes, wl.radius, precision=precision)
+        cap = full["n_pairs"] + 64
+        o = dict(node=np.empty(cap, np.uint32), prim=np.empty(cap, np.uint32), verdict=np.empty(cap, np.uint8),
+                 first_invalid=np.empty(cap, np.int16),
+                 end_state=np.empty((cap, nx), np.float64 if precision else np.float32),
+                 min_gap=None, flags=np.empty(cap, np.uint8))
+        r = ctx.expand(wl.nodes, wl.radius, precision=precision, capacity=cap, outputs=o)
+    assert r["n_pairs"] == full["n_pairs"]
+    for k in ("node", "prim", "verdict", "first_invalid", "end_state", "flags"):
+        np.testing.assert_array_equal(r[k], full[k])
+    ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius, fast=True, threads=ob.lib().orc_max_threads())
+    compare(wl.robot.kind, r, ora, precision, min_gap=False)
