@@ -447,6 +447,13 @@ def other_workload(args, lib, G, cfg, dev):
         del lazy
         m.pop("outs")
         m.pop("x_d")
+        # the same expand through the C ABI with page-locked host buffers
+        e2e = None
+        if not args.no_e2e:
+            e2e, pinned = run_e2e(args, lib, G, ctx, wl, m["cap"], n, wl.precision, 8 if wl.precision else 4, dev,
+                                  steps=min(args.steps, 10))
+            for h in pinned:
+                h.free()
     rec = {"workload": wl.name, "robot": wl.robot.name, "dtype": "f64" if wl.precision else "f32",
            "precision": {0: "DPG_FP32", 1: "DPG_FP64 (FP32 tests, FP64 band decisions and end states)"}[wl.precision],
            "primitives": wl.prims.P, "obstacles": len(wl.env.obs_lo), "nodes_per_step": len(wl.nodes),
@@ -457,6 +464,7 @@ def other_workload(args, lib, G, cfg, dev):
            "parity": "tests/test_parity_gpu.py::test_full_size_parity (every pair of this workload vs the oracle)",
            "roofline": {k: roof[k] for k in ("achieved", "peak", "unit", "frac")},
            **({"tuning": tune} if tune else {}),
+           **({"e2e": e2e} if e2e else {}),
            "lazy_vs_batched": {"limit_branching_factor": LIMIT_BRANCHING,
                                "rate": "in-ball candidate pairs handled per second (wall clock)",
                                "batched": {"value": n / t_e, "ms": 1e3 * t_e}, "batched_lazy": lz}}
@@ -803,9 +811,10 @@ def run_radius_variant(args, lib, ctx, wl, x_d, prec, dev):
             "checked_pairs_per_step": n_pairs, "ms_per_step": ms / args.steps}
 
 
-def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
+def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev, steps=None):
     """The C ABI with page-locked host buffers: H2D of the nodes, the expand,
     D2H of every output; wall clock per call."""
+    steps = args.steps if steps is None else steps
     N, nx = wl.nodes.shape
     xh = G.PinnedArray(wl.nodes.shape, np.float64)
     xh.array[:] = wl.nodes
@@ -821,7 +830,7 @@ def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
     for _ in range(args.warmup):
         ctx.expand(xh.array, wl.radius, precision=prec, capacity=cap, outputs=host_out)
     e2e_s, e2e_pairs = 0.0, 0
-    for _ in range(args.steps):
+    for _ in range(steps):
         lib.dpg_bench_flush_l2(dev, L2_FLUSH_BYTES)
         t0 = time.perf_counter()
         r = ctx.expand(xh.array, wl.radius, precision=prec, capacity=cap, outputs=host_out)
@@ -829,7 +838,7 @@ def run_e2e(args, lib, G, ctx, wl, cap, n_pairs, prec, es_bytes, dev):
         e2e_pairs += r["n_pairs"]
     d2h = n_pairs * (4 + 4 + 1 + 2 + es_bytes * nx + 1 + (4 if args.min_gap else 0))
     e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * nx * 8),
-           "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s / args.steps}
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s / steps}
     return e2e, list(hosts.values()) + [xh]
 
 

@@ -487,7 +487,7 @@ __device__ void check_one(const CheckArgs &A, const void *obs_sm, int p, int64_t
 // (every candidate is tested at every state up to the first contact).  FP32
 // tests with FP64 decisions in the band; the bounds tests stay per lane.
 
-constexpr int kSlotFill = 24;  // a narrow round stops taking chunks at this many slots
+constexpr int kSlotFill = 16;  // a narrow round stops taking chunks at this many slots
 
 template <int CH, int PARTS, int NW> struct SlotScratch {
   static constexpr int GMAX = 32 / CH;  // chunks a round can take (32 hit bits)

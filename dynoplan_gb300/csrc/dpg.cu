@@ -1038,8 +1038,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
 // the last call: the counters are cleared at the start of every call, and
 // calls whose device work overlaps (two streams, two host threads) race on it.
 // The first call on a device looks the array's device address up with
-// cudaGetSymbolAddress (once per device, with that device current); make that
-// first call before any stream capture.
+// cudaGetSymbolAddress (once per device, with that device current).
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;  // 64 MiB

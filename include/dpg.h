@@ -269,8 +269,7 @@ int dpg_lazy_check(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const d
  *     overlaps (other streams, other host threads, other contexts on the
  *     same GPU) race on it: serialise them.
  *   - The first call on a device looks the array's device address up
- *     (cudaGetSymbolAddress, with that device current); make that first
- *     call before any stream capture.
+ *     (cudaGetSymbolAddress, with that device current).
  *   - It honours DPG_MODE_BALL_ONLY; it does not update dpg_last_timings.
  * Results are identical to dpg_expand's with device outputs. */
 int dpg_expand_noalloc(dpg_ctx *ctx, const dpg_expand_opts *opts, int64_t N, const double *x_dev,
