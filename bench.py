@@ -55,11 +55,11 @@ L2_FLUSH_BYTES = 512 << 20
 # (profiles/check_pairs_car1_50k.md): sm__inst_executed.avg.per_cycle_active
 # over the SM's 4 issue slots per cycle, and warp instructions per pair.
 CHECK_ISSUE = {
-    2: {"inst_per_cycle": 2.916, "issue_slots": 4, "warp_instructions_per_pair": 1306890404 / 4126228,
-        "active_lanes_per_instruction": 13.93},
+    2: {"inst_per_cycle": 2.614, "issue_slots": 4, "warp_instructions_per_pair": 879676364 / 4126228,
+        "active_lanes_per_instruction": 17.68},
 }
 CHECK_TRAFFIC_PER_PAIR = {
-    2: (36.005632e6 + 63.423488e6) / 4126228,  # ncu capture (slot variant), car1_v0 with 50,000 nodes
+    2: (37.874944e6 + 51.243264e6) / 4126228,  # ncu capture (grouped slot rounds), car1_v0 with 50,000 nodes
 }
 
 
@@ -199,7 +199,7 @@ def part_boxes(wl, xs):
 
 
 def algorithmic_check_ops(wl, node, verdict, first_invalid, prim, sample=4000, seed=0,
-                          chunk=8, band=1e-4):
+                          chunk=8, band=1e-4, min_gap=False):
     """FP32 operations of the exact check of these pairs, counted for the
     algorithm check_pairs runs (two-level obstacle culling, separating-axis
     narrow phase), without any divergence or idle-lane waste, in the
@@ -214,9 +214,11 @@ def algorithmic_check_ops(wl, node, verdict, first_invalid, prim, sample=4000, s
       state
 
     collision-checked states: L (valid), first colliding + 1 (collision), 0
-    (out of bounds).  Also returns the lower bound any axis-aligned-broadphase
-    checker needs (F_NARROW per part-obstacle within GAP_CAP, no culling
-    levels).  Exact on a seeded sample of `sample` pairs, scaled to all."""
+    (out of bounds).  The culling margin is band + slack, plus GAP_CAP when
+    min_gap is an output.  Also returns the lower bound any axis-aligned-
+    broadphase checker needs (F_NARROW per part-obstacle within GAP_CAP with
+    min_gap, within the band without; no culling levels).  Exact on a seeded
+    sample of `sample` pairs, scaled to all."""
     m = wl.robot
     n = len(verdict)
     if n == 0:
@@ -226,7 +228,8 @@ def algorithmic_check_ops(wl, node, verdict, first_invalid, prim, sample=4000, s
     oc = 0.5 * (wl.env.obs_lo + wl.env.obs_hi)
     oh = 0.5 * (wl.env.obs_hi - wl.env.obs_lo)
     O, D = len(oc), wl.env.dim
-    M = GAP_CAP + band + 1e-3
+    cap = GAP_CAP if min_gap else band
+    M = (GAP_CAP if min_gap else 0.0) + band + 1e-3
     vel = {0: None, 1: None, 3: [3, 4], 2: [7, 8, 9]}[m.kind]
     cache = {}
     total = lower = 0
@@ -263,7 +266,7 @@ def algorithmic_check_ops(wl, node, verdict, first_invalid, prim, sample=4000, s
                 s1 = min(s_col, c1)
                 ops += (s1 - c0) * m.n_parts * (F_POSE + int(cand.sum()) * F_AABB)
                 ops += F_SAT * int((gap[c0:s1][:, :, cand] <= band).sum())
-            low += s_col * m.n_parts * F_POSE + F_NARROW * int((gap[:s_col] <= GAP_CAP).sum())
+            low += s_col * m.n_parts * F_POSE + F_NARROW * int((gap[:s_col] <= cap).sum())
         total += ops
         lower += low
     scale = n / len(idx)
@@ -385,7 +388,8 @@ def check_roofline(lib, wl, m, dev, cfg):
     fi = outs["first_invalid"][:n].cpu().numpy()
     prim = outs["prim"][:n].cpu().numpy()
     node = outs["node"][:n].cpu().numpy().view(np.uint32)
-    alg_ops, alg_lower = algorithmic_check_ops(wl, node, verdict, fi, prim, chunk=CHUNK_STATES[wl.robot.kind])
+    alg_ops, alg_lower = algorithmic_check_ops(wl, node, verdict, fi, prim, chunk=CHUNK_STATES[wl.robot.kind],
+                                               min_gap="min_gap" in outs)
     peak = ctypes_peak(lib, dev)
     achieved = alg_ops / m["check_s"] / 1e12
     return {"bound": "fp32", "kernel": "check_pairs", "achieved": achieved, "peak": peak,

@@ -29,8 +29,14 @@ struct TdbView {
   double delta;
 };
 
-// state k of motion p applied at node x (forward: start at the node;
-// reverse: the last state's position at the node's position)
+// state k of motion p applied at node x.  Forward: the motion starts at the
+// node.  Reverse: the motion ends at the node -- translation robots shift
+// the positions so that the last one is the node's; the rollout robots
+// (db-A*'s transform_primitiveDirectReverse, include/dynoplan/dbastar/
+// dbastar.hpp:183-201) take the offset (position, velocity) at the last
+// state: velocities shifted by dv = v_node - v_last, positions by
+// p_node - p_last + (t_k - t_last) dv, which is the same actions' rollout
+// from the shifted start (no dynamics term depends on position or velocity).
 template <int KIND>
 __device__ void tdb_state(const RobotParams &rp, const TdbView &tv, const double *x, int64_t s0, int L, int k,
                           double *out) {
@@ -38,10 +44,17 @@ __device__ void tdb_state(const RobotParams &rp, const TdbView &tv, const double
   const double *c = tv.st64 + (s0 + k) * R::NX;
 #pragma unroll
   for (int i = 0; i < R::NX; i++) out[i] = c[i];
-  if (tv.reverse) {  // translation robots only (checked on the host)
+  if (tv.reverse) {
     const double *last = tv.st64 + (s0 + L - 1) * R::NX;
+    const double tk = (k - (L - 1)) * rp.dt;  // time from the last state (<= 0)
 #pragma unroll
     for (int i = 0; i < R::POSD; i++) out[i] += x[i] - last[i];
+#pragma unroll
+    for (int i = 0; i < R::VELOFF; i++) {
+      const double dv = x[R::vel_comp(i)] - last[R::vel_comp(i)];
+      out[i] += tk * dv;
+      out[R::vel_comp(i)] += dv;
+    }
     return;
   }
   const double t = k * rp.dt;
@@ -137,10 +150,6 @@ extern "C" int dpg_tdb_check_pairs(dpg_ctx *c, const dpg_tdb_args *a, int64_t N,
   if (!c || !a || N < 0 || n < 0 || (n > 0 && (!x || !node || !prim || !verdict || !first_invalid))) return DPG_ERR_ARG;
   if (!c->have_prims || !c->have_env) return DPG_ERR_STATE;
   const int kind = c->robot.kind, nx = c->robot.nx;
-  if (a->reverse && (kind == DPG_ROBOT_QUAD2D || kind == DPG_ROBOT_QUAD3D)) {
-    c->err = "tdb_check_pairs: reverse expansion is defined for translation robots (unicycle1, car1)";
-    return DPG_ERR_ARG;
-  }
   if (a->n_constraints < 0 || (a->n_constraints > 0 && (!a->c_time || !a->c_state || !a->node_g || !a->goal)))
     return DPG_ERR_ARG;
   for (int64_t i = 0; i < n; i++)

@@ -6,9 +6,15 @@
  * 314-447) with LazyTraj::compute (include/dynoplan/tdbastar/
  * tdbastar.hpp:172-214):
  *   - forward: the motion starts at the node (the db-A* transform);
- *     reverse (translation robots only, as the reference's "assumes 2d"
- *     branch, :192-197): the motion is shifted so that its LAST state's
- *     position is the node's position (offset = node - last state);
+ *     reverse: the motion ends at the node -- translation robots as the
+ *     reference's "assumes 2d" branch (:192-197): shifted so that its LAST
+ *     state's position is the node's (offset = node - last state); quad2d
+ *     and quadrotor as db-A*'s reverse branch (transform_primitiveDirectReverse,
+ *     include/dynoplan/dbastar/dbastar.hpp:183-201; dynobench, absent,
+ *     restated): the last state takes the node's position and velocity,
+ *     every velocity moves by dv = v_node - v_last and every position by
+ *     p_node - p_last + (t_k - t_last) dv (the same actions rolled out from
+ *     the shifted start);
  *   - verdict as dpg_expand: any state out of bounds -> DPG_OUT_OF_BOUNDS,
  *     else the first colliding state -> DPG_COLLISION, else valid;
  *   - a valid motion is then tested against the constraints: for each

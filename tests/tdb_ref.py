@@ -1,18 +1,39 @@
 """Python restatement of tdb-A*'s check_lazy_trajectory
 (src/tdbastar/tdbastar.cpp:314-447, LazyTraj::compute tdbastar.hpp:172-214)
 over the oracle's bounds and separating-axis gap -- the checker of
-include/dpg_tdb.h, for the translation robots."""
+include/dpg_tdb.h (forward and reverse for the translation robots, reverse
+for quad2d and the quadrotor)."""
 import math
 
 import numpy as np
 
 import oracle_bind as ob
+from dynoplan_gb300 import workloads as W
+
+
+# position and velocity components of the rollout robots (the offset)
+_POS = {W.QUAD2D: [0, 1], W.QUAD3D: [0, 1, 2]}
+_VEL = {W.QUAD2D: [3, 4], W.QUAD3D: [7, 8, 9]}
 
 
 def _states(m, prims, p, x, reverse):
+    """The motion's states at node x.  Reverse: it ends at the node -- the
+    translation robots' position shift (tdbastar.hpp:192-197); for quad2d and
+    the quadrotor (db-A*'s transform_primitiveDirectReverse, dbastar.hpp:
+    183-201, restated) the last state takes the node's position and velocity,
+    velocities move by dv = v_node - v_last and positions by p_node - p_last +
+    (t_k - t_last) dv."""
     xs, _ = prims.motion(p)
     out = np.array(xs, float)
-    if reverse:
+    if m.kind in _VEL:
+        if not reverse:
+            raise NotImplementedError("forward transform of the rollout robots: compare with dpg_expand")
+        pc, vc = _POS[m.kind], _VEL[m.kind]
+        dv = np.asarray(x, float)[vc] - xs[-1][vc]
+        tk = (np.arange(len(xs)) - (len(xs) - 1)) * m.dt
+        out[:, pc] += np.asarray(x, float)[pc] - xs[-1][pc] + tk[:, None] * dv[None, :]
+        out[:, vc] += dv[None, :]
+    elif reverse:
         out[:, :2] += x[:2] - xs[-1, :2]
     else:
         out[:, :2] += x[:2]

@@ -1,6 +1,7 @@
 """tdb-A*'s pair checks (include/dpg_tdb.h): forward and reverse verdicts
 and the constraint test against tests/tdb_ref.py; the forward transform of
-the rollout robots against the regular FP64 check."""
+the rollout robots against the regular FP64 check, their reverse against
+the restatement."""
 import numpy as np
 import pytest
 
@@ -64,16 +65,34 @@ def test_tdb_forward_rollout_robots_match_check_pairs(dpg_lib, cfg):
     assert np.allclose(end, r["end_state"], rtol=0, atol=1e-9)
 
 
-def test_tdb_rejects_reverse_for_rollout_robots(dpg_lib):
+@pytest.mark.parametrize("cfg", [3, 5])
+def test_tdb_reverse_rollout_robots_match_restatement(dpg_lib, cfg):
+    """Reverse pairs of the rollout robots (quadrotor, quad2d): the motion
+    ends at the node with the node's position and velocity; verdicts, first
+    invalid states and end states against the FP64 restatement."""
     from dynoplan_gb300 import gpu as G
     from dynoplan_gb300 import tdb as T
-    from dynoplan_gb300._lib import DpgError
-    wl = W.make_workload(5, scale=0.005)
-    with G.Context(wl.robot) as ctx:
+    wl = W.make_workload(cfg, scale=0.01, seed=70 + cfg)
+    m = wl.robot
+    rng = np.random.default_rng(cfg)
+    n = 160
+    node = rng.integers(0, len(wl.nodes), n).astype(np.uint32)
+    prim = rng.integers(0, wl.prims.P, n).astype(np.uint32)
+    with G.Context(m) as ctx:
         ctx.upload_primitives(wl.prims)
         ctx.upload_env(wl.env)
-        with pytest.raises(DpgError):
-            T.check_pairs(ctx, wl.nodes, [0], [0], reverse=True)
+        v, fi, end = T.check_pairs(ctx, wl.nodes, node, prim, reverse=True)
+    ref = tdb_ref.check(m, wl.prims, wl.env, wl.nodes, np.zeros(len(wl.nodes), np.float32), node, prim, True,
+                        [], [], None, 0.0)
+    assert np.array_equal(v.astype(np.int64), ref[:, 0])
+    assert np.array_equal(fi.astype(np.int64), ref[:, 1])
+    assert len(set(v.tolist())) >= 2, "the sample must hold more than one verdict"
+    for i in range(n):
+        st = tdb_ref._states(m, wl.prims, int(prim[i]), wl.nodes[node[i]], True)
+        L = len(st)
+        k = fi[i] if v[i] == 2 else L - 1   # DPG_OUT_OF_BOUNDS: the end state is the first state out
+        assert np.allclose(end[i], st[k], rtol=0, atol=1e-9)
+        assert np.allclose(st[L - 1][:2], wl.nodes[node[i]][:2], atol=1e-9)   # it ends at the node
 
 
 @pytest.mark.parametrize("cfg", [1, 2])
