@@ -70,6 +70,7 @@ def test_tdb_reverse_rollout_robots_match_restatement(dpg_lib, cfg):
     """Reverse pairs of the rollout robots (quadrotor, quad2d): the motion
     ends at the node with the node's position and velocity; verdicts, first
     invalid states and end states against the FP64 restatement."""
+    import tdb_ref
     from dynoplan_gb300 import gpu as G
     from dynoplan_gb300 import tdb as T
     wl = W.make_workload(cfg, scale=0.01, seed=70 + cfg)
