@@ -23,11 +23,15 @@ def _states(m, prims, p, x, reverse):
     183-201, restated) the last state takes the node's position and velocity,
     velocities move by dv = v_node - v_last and positions by p_node - p_last +
     (t_k - t_last) dv."""
-    xs, _ = prims.motion(p)
+    xs, us = prims.motion(p)
     out = np.array(xs, float)
     if m.kind in _VEL:
         if not reverse:
             raise NotImplementedError("forward transform of the rollout robots: compare with dpg_expand")
+        # the canonical trajectory of a rollout robot is its actions rolled out
+        # from the stored start (as the library's upload does), not the stored states
+        xs = ob.rollout(m, xs[0], us)
+        out = np.array(xs, float)
         pc, vc = _POS[m.kind], _VEL[m.kind]
         dv = np.asarray(x, float)[vc] - xs[-1][vc]
         tk = (np.arange(len(xs)) - (len(xs) - 1)) * m.dt
