@@ -190,28 +190,37 @@ static __global__ void gather_rows(const float *rows, const int *sorted, int n, 
 
 // Block of 256 threads per query over the neighbouring cells (the 3 (2-D) or
 // 9 (3-D) runs of cells contiguous in the cell order; targets' FP32 rows in
-// cell order, so the loads are coalesced); lower_only: targets t < q.
-// Count pass (offset == nullptr): count[q] = the kept neighbours (all of them
-// without a filter), count_all[q] = every neighbour within the radius.  Write
-// pass: the kept neighbours' ids (and time lower bounds) at offset[q] + a slot
-// from the per-query counter fill[q] (zero on entry): the order within a list
-// is arbitrary, the host sorts each list by id.  Rewire filter (gsnap set):
-// a neighbour with g + lbt >= the g it entered the table with is dropped
-// (g only decreases, so it could never be rewired).
-// t_ok (lower_only queries): targets that can still be accepted as new nodes
-// this round; the others are skipped (a successor with an explored neighbour
-// in the radius and no goal hit is never accepted).
+// cell order, so the loads are coalesced); lower_only: targets t < q.  One
+// pass: count_all[q] = every neighbour within the radius, count[q] = the kept
+// ones (all of them without a filter), whose ids and time lower bounds are
+// collected in shared memory and written as one run at offset[q], a range
+// the block takes from the list counter *fill (the order of the runs, and
+// within a run, is arbitrary: the host sorts each list by id).  A query with
+// more kept neighbours than the shared buffer holds scans its cells again to
+// write them; runs past `cap` are not written (the host grows the lists and
+// repeats the round's queries).  Rewire filter (gsnap set): a neighbour with
+// g + lbt >= the g it entered the table with is dropped (g only decreases,
+// so it could never be rewired).  t_ok (lower_only queries): targets that can
+// still be accepted as new nodes this round; the others are skipped (a
+// successor with an explored neighbour in the radius and no goal hit is
+// never accepted).
+constexpr int kQueryBuf = 512;  // kept neighbours a query collects in shared memory
+
 template <int KIND>
 __global__ void __launch_bounds__(256) grid_query(RobotParams rp, float4 w32, Grid g, const double *q64,
                                                   const float *q32, int Q, const double *t64, const float *ts32,
                                                   const int *start, const int *cnt, const int *sorted, double radius,
                                                   float band, int lower_only, const unsigned char *t_ok,
-                                                  const double *gq, const float *gsnap, const int64_t *offset,
-                                                  int *count, int *count_all, int *fill, int *ids, double *lbt_out) {
+                                                  const double *gq, const float *gsnap, int *count, int *count_all,
+                                                  int64_t *offset, unsigned long long *fill, int64_t cap, int *ids,
+                                                  double *lbt_out) {
   using R = Robot<KIND>;
-  __shared__ int s_in, s_keep;
+  __shared__ int s_in, s_keep, s_put;
+  __shared__ int64_t s_at;
+  __shared__ int s_id[kQueryBuf];
+  __shared__ double s_lb[kQueryBuf];
   const int q = blockIdx.x;
-  if (threadIdx.x == 0) { s_in = 0; s_keep = 0; }
+  if (threadIdx.x == 0) { s_in = 0; s_keep = 0; s_put = 0; }
   __syncthreads();
   float a[R::NX];
 #pragma unroll
@@ -220,68 +229,86 @@ __global__ void __launch_bounds__(256) grid_query(RobotParams rp, float4 w32, Gr
 #pragma unroll
   for (int d = 0; d < R::POSD; d++) c0[d] = grid_coord<KIND>(g, a, d);
   const float gq32 = gq ? (float)gq[q] : 0.f;
-  int my_in = 0, my_keep = 0;
   const int zr = R::POSD == 3 ? 1 : 0;
-  for (int dz = -zr; dz <= zr; dz++)
-    for (int dy = -1; dy <= 1; dy++) {
-      const int cy = c0[1] + dy, cz = c0[2] + dz;
-      if (cy < 0 || cz < 0 || cy >= g.n[1] || (R::POSD == 3 && cz >= g.n[2])) continue;
-      const int x0 = max(c0[0] - 1, 0), x1 = min(c0[0] + 1, g.n[0] - 1);
-      const int row = g.n[0] * (cy + g.n[1] * cz);
-      const int s = start[row + x0], e = start[row + x1] + cnt[row + x1];
-      for (int j = s + (int)threadIdx.x; j < e; j += blockDim.x) {
-        const int t = sorted[j];
-        if (lower_only && (t >= q || (t_ok && !t_ok[t]))) continue;
-        const float *b = ts32 + (int64_t)j * R::NX;
-        float bb[R::NX];
+  // the neighbours of the cells around the query: fn(t, lb) for each kept one;
+  // returns this thread's count of neighbours within the radius
+  auto scan = [&](auto fn) -> int {
+    int my_in = 0;
+    for (int dz = -zr; dz <= zr; dz++)
+      for (int dy = -1; dy <= 1; dy++) {
+        const int cy = c0[1] + dy, cz = c0[2] + dz;
+        if (cy < 0 || cz < 0 || cy >= g.n[1] || (R::POSD == 3 && cz >= g.n[2])) continue;
+        const int x0 = max(c0[0] - 1, 0), x1 = min(c0[0] + 1, g.n[0] - 1);
+        const int row = g.n[0] * (cy + g.n[1] * cz);
+        const int s = start[row + x0], e = start[row + x1] + cnt[row + x1];
+        for (int j = s + (int)threadIdx.x; j < e; j += blockDim.x) {
+          const int t = sorted[j];
+          if (lower_only && (t >= q || (t_ok && !t_ok[t]))) continue;
+          const float *b = ts32 + (int64_t)j * R::NX;
+          float bb[R::NX];
 #pragma unroll
-        for (int k = 0; k < R::NX; k++) bb[k] = b[k];
-        const float d = full_dist32<KIND>(w32, a, bb);
-        bool in = d <= (float)radius;
-        if (fabsf(d - (float)radius) <= band)
-          in = full_dist64<KIND>(rp, q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX) <= radius;
-        if (!in) continue;
-        // (FP32 first: a neighbour clearly out by more than 1e-3 (1 + g) is
-        // dropped; the rest are decided, and their bound kept, in FP64)
-        bool keep = true, exact = lbt_out != nullptr && offset != nullptr;
-        double lb = 0.0;
-        if (gsnap) {
-          const float gs = gsnap[t];
-          if (gq32 + lbt32<KIND>(a, bb) > gs + 1e-3f * (1.f + fabsf(gs))) {
-            keep = false;
-            exact = false;
-          } else {
-            exact = true;
+          for (int k = 0; k < R::NX; k++) bb[k] = b[k];
+          const float d = full_dist32<KIND>(w32, a, bb);
+          bool in = d <= (float)radius;
+          if (fabsf(d - (float)radius) <= band)
+            in = full_dist64<KIND>(rp, q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX) <= radius;
+          if (!in) continue;
+          // (FP32 first: a neighbour clearly out by more than 1e-3 (1 + g) is
+          // dropped; the rest are decided, and their bound kept, in FP64)
+          bool keep = true, exact = lbt_out != nullptr;
+          double lb = 0.0;
+          if (gsnap) {
+            const float gs = gsnap[t];
+            if (gq32 + lbt32<KIND>(a, bb) > gs + 1e-3f * (1.f + fabsf(gs))) {
+              keep = false;
+              exact = false;
+            } else {
+              exact = true;
+            }
           }
-        }
-        if (exact) {
-          lb = lbt_exact<KIND>(q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX);
-          if (gsnap) keep = __dadd_rn(gq[q], lb) < (double)gsnap[t];
-        }
-        my_in++;
-        if (!keep) continue;
-        my_keep++;
-        if (offset) {
-          const int64_t at = offset[q] + atomicAdd(&fill[q], 1);
-          ids[at] = t;
-          if (lbt_out) lbt_out[at] = lb;
+          if (exact) {
+            lb = lbt_exact<KIND>(q64 + (int64_t)q * R::NX, t64 + (int64_t)t * R::NX);
+            if (gsnap) keep = __dadd_rn(gq[q], lb) < (double)gsnap[t];
+          }
+          my_in++;
+          if (keep) fn(t, lb);
         }
       }
+    return my_in;
+  };
+  int my_in = scan([&](int t, double lb) {
+    const int slot = atomicAdd(&s_keep, 1);
+    if (slot < kQueryBuf) {
+      s_id[slot] = t;
+      s_lb[slot] = lb;
     }
-  if (!offset) {
-    for (int o = 16; o > 0; o >>= 1) {
-      my_in += __shfl_down_sync(0xffffffffu, my_in, o);
-      my_keep += __shfl_down_sync(0xffffffffu, my_keep, o);
+  });
+  for (int o = 16; o > 0; o >>= 1) my_in += __shfl_down_sync(0xffffffffu, my_in, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&s_in, my_in);
+  __syncthreads();
+  const int n = s_keep;
+  if (threadIdx.x == 0) {
+    s_at = (int64_t)atomicAdd(fill, (unsigned long long)n);
+    count[q] = n;
+    if (count_all) count_all[q] = s_in;
+    offset[q] = s_at;
+  }
+  __syncthreads();
+  const int64_t at = s_at;
+  if (at + n > cap) return;  // the host grows the lists and repeats the queries
+  if (n <= kQueryBuf) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      ids[at + i] = s_id[i];
+      if (lbt_out) lbt_out[at + i] = s_lb[i];
     }
-    if ((threadIdx.x & 31) == 0) {
-      atomicAdd(&s_in, my_in);
-      atomicAdd(&s_keep, my_keep);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      count[q] = s_keep;
-      if (count_all) count_all[q] = s_in;
-    }
+  } else {  // more than the buffer: the same scan again, writing straight to the list
+    scan([&](int t, double lb) {
+      const int slot = atomicAdd(&s_put, 1);
+      if (slot < n) {
+        ids[at + slot] = t;
+        if (lbt_out) lbt_out[at + slot] = lb;
+      }
+    });
   }
 }
 
@@ -494,7 +521,6 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   }
   // cell-sorted copies of the explored nodes (t_*) and of a round's successors (s_*)
   DVec<int> tab_cnt, tab_start, tab_fill, tab_cell, tab_sorted, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted;
-  DVec<int> fill_tab, fill_self;
   DVec<unsigned char> ok_d;
   DVec<float> tab_rows, rnd_rows;
   if (!tab_cnt.reserve(n_cells) || !tab_start.reserve(n_cells) || !tab_fill.reserve(n_cells) ||
@@ -566,6 +592,7 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
   DVec<float> q32;
   DVec<int> cnt_tab, ids_tab, cnt_self, ids_self;
   DVec<int64_t> off_tab, off_self;
+  DVec<unsigned long long> list_fill;  // the two lists' counters
   DVec<uint32_t> pnode, pprim;
   DVec<float> mlp_out;
   DVec<__nv_bfloat16> feat;
@@ -727,54 +754,51 @@ extern "C" int dpg_search(dpg_ctx *c, const dpg_search_opts *o, const double *st
       res->table_ms += elapsed_ms() - tt0;
       // the round's successors sorted by cell too, for the lower-index query
       if (!sort_by_cell(q32.p, Q, rnd_cnt, rnd_start, rnd_fill, rnd_cell, rnd_sorted, rnd_rows) ||
-          !fill_tab.reserve(Q) || !fill_self.reserve(Q) || !ok_d.reserve(Q))
+          !ok_d.reserve(Q))
         return DPG_ERR_OOM;
-      // count pass, offsets on the host, write pass into packed lists: the
-      // explored neighbours that pass the rewire filter (all of them are
-      // counted for the novelty test) and every earlier successor of the
-      // round within the radius, each with its time lower bound
+      // one pass per query set: the explored neighbours that pass the rewire
+      // filter (all of them are counted for the novelty test) and every
+      // earlier successor of the round within the radius, each with its time
+      // lower bound, in packed lists (a run per query, offsets from the device)
       std::vector<int> ct(Q), ca(Q), cs(Q), it, is;
       std::vector<double> lt, ls;
       std::vector<int64_t> ot(Q), os(Q);
-      auto query = [&](const int64_t *off_t, const int64_t *off_s) {  // a block per query
-        if (off_t) {
-          cudaMemsetAsync(fill_tab.p, 0, sizeof(int) * Q);
-          cudaMemsetAsync(fill_self.p, 0, sizeof(int) * Q);
-        }
+      unsigned long long nts[2] = {0, 0};
+      if (!off_tab.reserve(Q) || !off_self.reserve(Q) || !list_fill.reserve(2)) return DPG_ERR_OOM;
+      auto query = [&]() {  // a block per query
+        cudaMemsetAsync(list_fill.p, 0, sizeof(unsigned long long) * 2);
         with_kind_s(r.kind, [&](auto Kd) {
           constexpr int KIND = decltype(Kd)::value;
           grid_query<KIND><<<(unsigned)Q, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, t64.p, tab_rows.p, tab_start.p,
                                                  tab_cnt.p, tab_sorted.p, nov_radius, 1e-5f, 0, nullptr, gq.p,
-                                                 gsnap.p, off_t, cnt_tab.p, cnt_all.p, fill_tab.p, ids_tab.p,
-                                                 lbt_tab.p);
+                                                 gsnap.p, cnt_tab.p, cnt_all.p, off_tab.p, list_fill.p,
+                                                 (int64_t)std::min(ids_tab.cap, lbt_tab.cap), ids_tab.p, lbt_tab.p);
           // which successors can be accepted follows from the explored-table counts
-          if (!off_t) acceptable<<<(Q + 255) / 256, 256>>>(Q, cnt_all.p, prep.p, (int)prow, nx, ok_d.p);
+          acceptable<<<(Q + 255) / 256, 256>>>(Q, cnt_all.p, prep.p, (int)prow, nx, ok_d.p);
           grid_query<KIND><<<(unsigned)Q, 256>>>(c->rp, w32, grid, q64.p, q32.p, Q, q64.p, rnd_rows.p, rnd_start.p,
                                                  rnd_cnt.p, rnd_sorted.p, nov_radius, 1e-5f, 1, ok_d.p, nullptr,
-                                                 nullptr, off_s, cnt_self.p, nullptr, fill_self.p, ids_self.p,
+                                                 nullptr, cnt_self.p, nullptr, off_self.p, list_fill.p + 1,
+                                                 (int64_t)std::min(ids_self.cap, lbt_self.cap), ids_self.p,
                                                  lbt_self.p);
         });
+        return cudaMemcpy(nts, list_fill.p, sizeof(nts), cudaMemcpyDeviceToHost) == cudaSuccess;
       };
       const double tq0 = elapsed_ms();
-      query(nullptr, nullptr);
+      if (!ids_tab.reserve(1024) || !lbt_tab.reserve(1024) || !ids_self.reserve(1024) || !lbt_self.reserve(1024) ||
+          !query())
+        return DPG_ERR_CUDA;
+      if (nts[0] > std::min(ids_tab.cap, lbt_tab.cap) || nts[1] > std::min(ids_self.cap, lbt_self.cap)) {
+        // lists past the capacity: grow them, query again
+        if (!ids_tab.reserve(nts[0]) || !lbt_tab.reserve(nts[0]) || !ids_self.reserve(nts[1]) ||
+            !lbt_self.reserve(nts[1]) || !query())
+          return DPG_ERR_OOM;
+      }
+      const int64_t nt = (int64_t)nts[0], ns = (int64_t)nts[1];
       cudaMemcpy(ct.data(), cnt_tab.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
       cudaMemcpy(ca.data(), cnt_all.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
-      if (cudaMemcpy(cs.data(), cnt_self.p, sizeof(int) * Q, cudaMemcpyDeviceToHost) != cudaSuccess)
-        return DPG_ERR_CUDA;
-      int64_t nt = 0, ns = 0;
-      for (int i = 0; i < Q; i++) {
-        ot[i] = nt;
-        os[i] = ns;
-        nt += ct[i];
-        ns += cs[i];
-      }
-      if (!ids_tab.reserve((size_t)std::max<int64_t>(nt, 1)) || !ids_self.reserve((size_t)std::max<int64_t>(ns, 1)) ||
-          !lbt_tab.reserve((size_t)std::max<int64_t>(nt, 1)) || !lbt_self.reserve((size_t)std::max<int64_t>(ns, 1)) ||
-          !off_tab.reserve(Q) || !off_self.reserve(Q))
-        return DPG_ERR_OOM;
-      cudaMemcpy(off_tab.p, ot.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice);
-      cudaMemcpy(off_self.p, os.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice);
-      query(off_tab.p, off_self.p);
+      cudaMemcpy(cs.data(), cnt_self.p, sizeof(int) * Q, cudaMemcpyDeviceToHost);
+      cudaMemcpy(ot.data(), off_tab.p, sizeof(int64_t) * Q, cudaMemcpyDeviceToHost);
+      cudaMemcpy(os.data(), off_self.p, sizeof(int64_t) * Q, cudaMemcpyDeviceToHost);
       it.resize((size_t)nt);
       is.resize((size_t)ns);
       lt.resize((size_t)nt);

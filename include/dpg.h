@@ -141,7 +141,8 @@ typedef struct dpg_expand_out {
   uint8_t *verdict;        /* DPG_VALID / DPG_COLLISION / DPG_OUT_OF_BOUNDS */
   int16_t *first_invalid;  /* first out-of-bounds or colliding state, or L */
   void *end_state;         /* n_pairs x nx, float (DPG_FP32) or double (DPG_FP64, _STRICT) */
-  float *min_gap;          /* min axis-aligned clearance along the checked states */
+  float *min_gap;          /* min axis-aligned clearance along the checked states (costs check
+                              time: per-state gap merges and a wider culling margin) */
   uint8_t *flags;          /* DPG_FLAG_* */
   /* counters (out) */
   int64_t n_scanned;       /* node x primitive ball tests */

@@ -353,3 +353,29 @@ def test_min_gap_optional(gpu, cfg, scale, precision):
         np.testing.assert_array_equal(r[k], full[k])
     ora = ob.expand(wl.robot, wl.prims, wl.env, wl.nodes, wl.radius, fast=True, threads=ob.lib().orc_max_threads())
     compare(wl.robot.kind, r, ora, precision, min_gap=False)
+
+
+@pytest.mark.parametrize("n_obs", [32, 33, 96, 97, 128, 129, 300])
+def test_obstacle_counts_around_mask_words(gpu, n_obs):
+    """Obstacle counts at the edges of the candidate bitmask words (32 a word,
+    culling up to 128, every obstacle tested above that): the results equal
+    the oracle's for both narrow phases, with and without min_gap."""
+    m = W.robot_model(W.CAR1)
+    env = W.make_env((10.0, 10.0), n_obs, 0.1, 0.6, seed=900 + n_obs)
+    nodes = W.make_nodes(m, env, 2500, seed=901)
+    prims = W.make_primitives(m, 80, 5, 60, seed=902)
+    ora = ob.expand(m, prims, env, nodes, 0.5, fast=True, threads=ob.lib().orc_max_threads())
+    assert (ora["verdict"] == 1).any() and (ora["verdict"] == 0).any()
+    with gpu.Context(m) as ctx:
+        ctx.upload_primitives(prims)
+        ctx.upload_env(env)
+        for variant in (0, 1):
+            ctx.set_tuning(check_variant=variant)
+            res = ctx.expand(nodes, 0.5)
+            compare(W.CAR1, res, ora, 0)
+            cap = res["n_pairs"] + 64
+            o = dict(node=np.empty(cap, np.uint32), prim=np.empty(cap, np.uint32), verdict=np.empty(cap, np.uint8),
+                     first_invalid=np.empty(cap, np.int16), end_state=np.empty((cap, 4), np.float32),
+                     min_gap=None, flags=np.empty(cap, np.uint8))
+            r2 = ctx.expand(nodes, 0.5, capacity=cap, outputs=o)
+            compare(W.CAR1, r2, ora, 0, min_gap=False)
