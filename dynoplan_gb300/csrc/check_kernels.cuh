@@ -499,6 +499,8 @@ template <int CH, int PARTS, int NW> struct SlotScratch {
   unsigned mg[MGS][32];                 // per state and lane: min axis-aligned gap (order-preserving bits)
   unsigned hit[32];                     // per lane: bit s = contact at state k0 + s
   unsigned rc[32];                      // per lane: bit s = a test at k0 + s was decided in FP64
+  // (the bounds slots of a chunk use hit / rc before the narrow phase does:
+  // bit j = state j of the chunk out of bounds / decided in FP64)
 };
 
 __device__ __forceinline__ unsigned ord_gap(float f) {
@@ -638,9 +640,63 @@ __device__ void check_one_slots(const CheckArgs &A, const void *obs_sm,
           nb = !in;
         }
       }
-      // bounds tests of the chunk's states, per lane, up to the first state out
+      // bounds tests of the chunk's states, up to each lane's first state out.
+      // Few lanes with tests: (lane, state) slots over the warp, each lane's
+      // first state out (and the FP64 decisions up to it) from bitmasks, as
+      // the sequential walk finds them; else each lane walks its states.
       int j_oob = CH;
-      if (nb) {
+      bool walk = nb;
+      if constexpr (R::BOUNDS_SLOTS) {
+        const unsigned nbm = __ballot_sync(kFull, nb);
+        const int nbs = __popc(nbm) * (kend - kk);
+        if (nbm && nbs <= 64) {
+          walk = false;
+          const int ns = kend - kk;
+          S.hit[lane] = 0u;
+          S.rc[lane] = 0u;
+          __syncwarp();
+          for (int base = 0; base < nbs; base += 32) {
+            const int t = base + lane;
+            const int li = t / ns, j = t - li * ns;
+            const int owner = t < nbs ? (int)__fns(nbm, 0u, li + 1) : 0;
+            float osh[D + V];
+  #pragma unroll
+            for (int i = 0; i < D + V; i++) osh[i] = __shfl_sync(kFull, off[i], owner);
+            const uint32_t onode = __shfl_sync(kFull, node, owner);
+            if (t < nbs) {
+              const int k = kk + j;
+              const Pose<float> ps = pose[s0 + k];  // part 0 = the state position
+              const float tk = float(k) * dt;
+              const float pv3[3] = {ps.cx + osh[0] + (V ? tk * osh[D] : 0.f), ps.cy + osh[1] + (V ? tk * osh[D + 1] : 0.f),
+                                    D == 3 ? ps.c + osh[2] + (V ? tk * osh[D + 2] : 0.f) : 0.f};
+              int bt = 0;
+              bool amb = false;
+  #pragma unroll
+              for (int i = 0; i < D; i++) {
+                const float v = pv3[i], lo = A.lo32[i], hi = A.hi32[i];
+                int r = (v < lo - band || v > hi + band) ? 1 : ((v <= lo + band || v >= hi - band) ? 2 : 0);
+                if (r == 2) {  // decide in FP64
+                  const double v64 = pos64<KIND>(A, s0 + k, k, A.nv.x64 + (int64_t)onode * R::NX, i);
+                  r = (v64 >= A.ev.lo[i] && v64 <= A.ev.hi[i]) ? 0 : 1;
+                  amb = true;
+                }
+                bt |= r;
+              }
+              if (bt) atomicOr(&S.hit[owner], 1u << j);
+              if (amb) atomicOr(&S.rc[owner], 1u << j);
+            }
+          }
+          __syncwarp();
+          if (nb) {
+            const unsigned bo = S.hit[lane];
+            const int first = bo ? __ffs(bo) - 1 : CH;
+            if (bo) j_oob = first;
+            if (S.rc[lane] & (bo ? ((2u << first) - 1u) : 0xffffffffu)) rechecked = true;
+          }
+          __syncwarp();  // the next chunk's slots and the narrow phase reuse the masks
+        }
+      }
+      if (walk) {
         for (int k = kk; k < kend; k++) {
           const Pose<float> ps = pose[s0 + k];  // part 0 = the state position
           const float t = float(k) * dt;

@@ -364,7 +364,7 @@ def test_obstacle_counts_around_mask_words(gpu, n_obs):
     env = W.make_env((10.0, 10.0), n_obs, 0.1, 0.6, seed=900 + n_obs)
     nodes = W.make_nodes(m, env, 2500, seed=901)
     prims = W.make_primitives(m, 80, 5, 60, seed=902)
-    ora = ob.expand(m, prims, env, nodes, 0.5, fast=True, threads=ob.lib().orc_max_threads())
+    ora = ob.expand(m, prims, env, nodes, 0.5)   # the reference oracle (min_gap included)
     assert (ora["verdict"] == 1).any() and (ora["verdict"] == 0).any()
     with gpu.Context(m) as ctx:
         ctx.upload_primitives(prims)
