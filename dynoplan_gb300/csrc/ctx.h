@@ -58,6 +58,8 @@ struct dpg_ctx {
   cudaEvent_t ev_ball = nullptr;
   cudaEvent_t ev_sub[dpg::kMaxSub] = {};
   cudaEvent_t ev_tot = nullptr;
+  cudaEvent_t ev_cl[2] = {};  // around the last copy range of a host-buffer expand
+  double pipe_decay = 0.75;   // each copy range this fraction of the one before (adapted per call)
   unsigned long long *h_bases = nullptr;  // [2][h_bases_n]: ord_ibase, ord_pbase
   size_t h_bases_n = 0;
   // dpg_lazy_check: candidates by node, ranks, cursors, round lists, counters

@@ -177,16 +177,18 @@ static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
 // (an expand whose results go to host buffers runs tune.pipe_launches <=
 // kMaxSub check launches, one work-queue counter each)
 
-// Cumulative item weights of the pipelined check launches: each range
-// 3/4 the size of the one before, so a range's result copy (about half as
-// long as its check on car1) overlaps the next range's check and the last,
-// exposed copy is small.  cum[0] = 0, cum[n] = the total.
-static void pipe_weights(int n, int *cum) {
+// Cumulative item weights of the copy ranges of a host-buffer expand: each
+// range `decay` times the one before, so a range's result copy overlaps the
+// next ranges' check and the last, exposed copy is small.  The decay follows
+// the ratio of copy time to check time (dpg_expand adapts it after each call:
+// car1's copies take about 0.6 of its check, so 3/4; the quadrotor's about as
+// long as its check, so equal ranges).  cum[0] = 0, cum[n] = the total.
+static void pipe_weights(int n, int *cum, double decay) {
   cum[0] = 0;
   double w = 1000.0;
   for (int j = 0; j < n; j++) {
     cum[j + 1] = cum[j] + (int)w;
-    w *= 0.75;
+    w *= decay;
   }
 }
 template <int KIND>
@@ -346,6 +348,8 @@ void dpg_destroy(dpg_ctx *c) {
     if (e) cudaEventDestroy(e);
   if (c->ev_tot) cudaEventDestroy(c->ev_tot);
   if (c->ev_ball) cudaEventDestroy(c->ev_ball);
+  for (auto &e : c->ev_cl)
+    if (e) cudaEventDestroy(e);
   if (c->cstream) cudaStreamDestroy(c->cstream);
   if (c->xstream) cudaStreamDestroy(c->xstream);
   if (c->h_abort) cudaFreeHost(c->h_abort);
@@ -772,6 +776,8 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   // one check launch whose warps flag finished copy ranges in mapped memory
   const bool progress = pipelined && c->tune.host_output == DPG_HOST_OUT_PROGRESS;
   const int n_ranges = pipelined ? c->tune.pipe_launches : 1;
+  const double decay = c->pipe_decay;  // the copy ranges' sizes for this call
+  size_t last_bytes = 0;               // bytes of the last range's copies
   if (progress && !c->h_rflag) {
     CUDA_TRY(c, cudaHostAlloc(&c->h_rflag, sizeof(int) * kMaxSub, cudaHostAllocMapped));
     CUDA_TRY(c, cudaHostGetDevicePointer(&c->d_rflag, c->h_rflag, 0));
@@ -785,6 +791,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       for (auto &e : c->ev_sub) CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
       CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_tot, cudaEventDisableTiming));
       CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_ball, cudaEventDisableTiming));
+      for (auto &e : c->ev_cl) CUDA_TRY(c, cudaEventCreate(&e));
     }
     if (c->h_bases_n < (size_t)P + 1) {
       if (c->h_bases) cudaFreeHost(c->h_bases);
@@ -921,7 +928,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       ca.nsub = pipelined && !progress ? n_ranges : 1;
       ca.n_ranges = progress ? n_ranges : 0;
       ca.range_flag = progress ? c->d_rflag : nullptr;
-      pipe_weights(n_ranges, ca.sub_cum);
+      pipe_weights(n_ranges, ca.sub_cum, decay);
       for (int j = 0; j < ca.nsub; j++) {
         ca.sub = j;
         cudaStream_t s = pipelined && (j & 1) ? c->xstream : st;
@@ -960,7 +967,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
           {out->min_gap, c->p_gap.p, 4}, {out->flags, c->p_flags.p, 1}};
       const int np = n_ranges;
       int cum[kMaxSub + 1];
-      pipe_weights(np, cum);
+      pipe_weights(np, cum, decay);
       for (int j = 0; j < np; j++) {
         const int64_t a = pair_at(h0.n_items * cum[j] / cum[np]), e = pair_at(h0.n_items * cum[j + 1] / cum[np]);
         if (progress) {
@@ -972,11 +979,15 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
         } else {
           CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev_sub[j], 0));
         }
+        if (j == np - 1) CUDA_TRY(c, cudaEventRecord(c->ev_cl[0], c->cstream));
         if (e > a)
           for (const auto &f : cp)
-            if (f.dst)
+            if (f.dst) {
               CUDA_TRY(c, cudaMemcpyAsync(static_cast<char *>(f.dst) + a * f.b, static_cast<char *>(f.src) + a * f.b,
                                           (e - a) * f.b, cudaMemcpyDeviceToHost, c->cstream));
+              if (j == np - 1) last_bytes += (e - a) * f.b;
+            }
+        if (j == np - 1) CUDA_TRY(c, cudaEventRecord(c->ev_cl[1], c->cstream));
       }
     }
     CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev[4], 0));
@@ -1016,6 +1027,20 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   cudaEventElapsedTime(&t_in, c->ev[0], c->ev[1]);
   cudaEventElapsedTime(&t_out, c->ev[4], c->ev[5]);
   c->timings[3] = t_in + t_out;
+  if (pipelined && last_bytes >= (1u << 20) && np > 0 && c->timings[1] > 0) {
+    // the next call's range decay: this call's copy time (at the rate of its
+    // last range, whose copies run after the check) over its check time
+    float cl = 0;
+    if (cudaEventElapsedTime(&cl, c->ev_cl[0], c->ev_cl[1]) == cudaSuccess && cl > 0) {
+      size_t bpp = 0;  // bytes copied per pair
+      const size_t b1[7] = {4, 4, 1, 2, (size_t)es_bytes * nx, 4, 1};
+      void *d1[7] = {out->node, out->prim, out->verdict, out->first_invalid, out->end_state, out->min_gap, out->flags};
+      for (int i = 0; i < 7; i++)
+        if (d1[i]) bpp += b1[i];
+      const double copy_ms = (double)bpp * (double)np * (double)cl / (double)last_bytes;
+      c->pipe_decay = std::min(1.0, std::max(0.75, copy_ms / (double)c->timings[1]));
+    }
+  }
   return DPG_OK;
 }
 
