@@ -177,6 +177,8 @@ static int nn_tiles_per_y(int P, int64_t B, int sm_count) {
 // (an expand whose results go to host buffers runs tune.pipe_launches <=
 // kMaxSub check launches, one work-queue counter each)
 
+constexpr size_t kMinCopyBytes = 16u << 20;  // smallest group of copy ranges copied together
+
 // Cumulative item weights of the copy ranges of a host-buffer expand: each
 // range `decay` times the one before, so a range's result copy overlaps the
 // next ranges' check and the last, exposed copy is small.  The decay follows
@@ -968,6 +970,13 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       const int np = n_ranges;
       int cum[kMaxSub + 1];
       pipe_weights(np, cum, decay);
+      size_t bpp = 0;  // bytes copied per pair
+      for (const auto &f : cp)
+        if (f.dst) bpp += f.b;
+      // consecutive ranges are copied together until a group holds
+      // kMinCopyBytes (each copy call costs host time; small batches get
+      // fewer, larger copies); the last range closes the last group
+      int64_t ga = -1;
       for (int j = 0; j < np; j++) {
         const int64_t a = pair_at(h0.n_items * cum[j] / cum[np]), e = pair_at(h0.n_items * cum[j + 1] / cum[np]);
         if (progress) {
@@ -979,15 +988,19 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
         } else {
           CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev_sub[j], 0));
         }
-        if (j == np - 1) CUDA_TRY(c, cudaEventRecord(c->ev_cl[0], c->cstream));
-        if (e > a)
+        if (ga < 0) ga = a;
+        const bool last = j == np - 1;
+        if (!last && (size_t)(e - ga) * bpp < kMinCopyBytes) continue;
+        if (last) CUDA_TRY(c, cudaEventRecord(c->ev_cl[0], c->cstream));
+        if (e > ga)
           for (const auto &f : cp)
             if (f.dst) {
-              CUDA_TRY(c, cudaMemcpyAsync(static_cast<char *>(f.dst) + a * f.b, static_cast<char *>(f.src) + a * f.b,
-                                          (e - a) * f.b, cudaMemcpyDeviceToHost, c->cstream));
-              if (j == np - 1) last_bytes += (e - a) * f.b;
+              CUDA_TRY(c, cudaMemcpyAsync(static_cast<char *>(f.dst) + ga * f.b, static_cast<char *>(f.src) + ga * f.b,
+                                          (e - ga) * f.b, cudaMemcpyDeviceToHost, c->cstream));
+              if (last) last_bytes += (e - ga) * f.b;
             }
-        if (j == np - 1) CUDA_TRY(c, cudaEventRecord(c->ev_cl[1], c->cstream));
+        if (last) CUDA_TRY(c, cudaEventRecord(c->ev_cl[1], c->cstream));
+        ga = -1;
       }
     }
     CUDA_TRY(c, cudaStreamWaitEvent(c->cstream, c->ev[4], 0));
