@@ -40,8 +40,8 @@ METRIC = "checked (node,primitive) expansions/s"
 UNIT = "pairs/s"
 # node_tiles nn_prefix cell_scan cell_scatter gather_nodes (spatial order, batches of
 # >= 2048 nodes) prep_nodes nn_grid (key-grid ball scan; nn_mask for the quadrotor)
-# nn_prefix scan_totals nn_emit check_pairs (which also restores the node ids)
-KERNELS_PER_STEP = 11
+# nn_prefix scan_totals item_positions nn_emit check_pairs (which also restores the node ids)
+KERNELS_PER_STEP = 12
 # states per culling chunk of check_pairs by robot kind (the kernel's
 # Robot<KIND>::CHUNK): unicycle1 0, car1 1, quadrotor 2, quad2d 3
 CHUNK_STATES = {0: 8, 1: 8, 2: 16, 3: 16}

@@ -43,6 +43,7 @@ struct CheckArgs {
   PairView out;
   const unsigned long long *ord_pbase;
   const unsigned long long *ord_ibase;
+  const uint32_t *item_pos;  // item -> order position (null: binary search over ord_ibase)
   DevCounters *ctr;
   const volatile int *abort_flag;
   double band;       // FP64 re-check band (0 on the FP64 path)
@@ -994,10 +995,15 @@ __global__ void __launch_bounds__(kCheckThreads, SLOTS ? Robot<KIND>::SLOT_BLOCK
       cur_cnt++;
     }
     // order position lo with ord_ibase[lo] <= item < ord_ibase[lo + 1]
-    int lo = 0, hi = P;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (A.ord_ibase[mid] <= item) lo = mid; else hi = mid;
+    int lo = 0;
+    if (A.item_pos) {
+      lo = (int)A.item_pos[item];
+    } else {
+      int hi = P;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (A.ord_ibase[mid] <= item) lo = mid; else hi = mid;
+      }
     }
     const int p = A.pv.order[lo];
     const unsigned long long j = item - A.ord_ibase[lo];

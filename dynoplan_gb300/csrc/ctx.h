@@ -46,6 +46,7 @@ struct dpg_ctx {
 
   // per-call arena
   DevBuf x64, nkey32, noff32, mask, cnt, tot, pbase, ord_pbase, ord_ibase;
+  DevBuf item_pos;  // work item -> its primitive's position in length order
   DevBuf p_node, p_prim, p_verdict, p_fi, p_end, p_gap, p_flags;
   DevBuf q_node, q_prim, q_sorted, q_idx, q_fill;  // dpg_check_pairs
   DevBuf ord_cell, ord_perm, ord_cnt, ord_start, ord_rank, ord_tiles, x64s;  // spatial order of a batch

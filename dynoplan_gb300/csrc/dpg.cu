@@ -334,7 +334,7 @@ void dpg_destroy(dpg_ctx *c) {
   DevBuf *bufs[] = {&c->len, &c->soff, &c->aoff, &c->order, &c->key32, &c->kconst32, &c->st64,
                     &c->st32, &c->act64, &c->pose32, &c->pose64, &c->pbox, &c->pbox32, &c->obs32, &c->obs64,
                     &c->x64, &c->nkey32, &c->noff32, &c->mask, &c->cnt, &c->tot, &c->pbase,
-                    &c->ord_pbase, &c->ord_ibase, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
+                    &c->ord_pbase, &c->ord_ibase, &c->item_pos, &c->p_node, &c->p_prim, &c->p_verdict, &c->p_fi,
                     &c->p_end, &c->p_gap, &c->p_flags, &c->coff, &c->cbox32, &c->tbox32,
                     &c->q_node, &c->q_prim, &c->q_sorted, &c->q_idx, &c->q_fill,
                     &c->ord_cell, &c->ord_perm, &c->ord_cnt, &c->ord_start, &c->ord_rank, &c->ord_tiles, &c->x64s,
@@ -701,7 +701,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
       (rc = ensure(c, c->tot, sizeof(uint32_t) * P)) ||
       (rc = ensure(c, c->pbase, sizeof(unsigned long long) * P)) ||
       (rc = ensure(c, c->ord_pbase, sizeof(unsigned long long) * (P + 1))) ||
-      (rc = ensure(c, c->ord_ibase, sizeof(unsigned long long) * (P + 1))))
+      (rc = ensure(c, c->ord_ibase, sizeof(unsigned long long) * (P + 1))) ||
+      // work items: at most one per 32 pairs of the capacity plus one partial item per primitive
+      (rc = ensure(c, c->item_pos, sizeof(uint32_t) * (size_t)(std::max<int64_t>(cap, 0) / 32 + P + 1))))
     return rc;
   // batches of at least kReorderMin nodes are processed in spatial order
   const bool reorder = N >= kReorderMin;
@@ -857,6 +859,7 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
   ca.out = pv_out;
   ca.ord_pbase = P_<unsigned long long>(c->ord_pbase);
   ca.ord_ibase = P_<unsigned long long>(c->ord_ibase);
+  ca.item_pos = P_<uint32_t>(c->item_pos);
   ca.ctr = ctr;
   ca.abort_flag = c->d_abort;
   ca.band = fp64 ? 0.0 : band;
@@ -898,6 +901,9 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
     scan_totals<<<1, 1024, 0, st>>>(P, P_<int32_t>(c->order), P_<uint32_t>(c->tot),
                                     P_<unsigned long long>(c->pbase), P_<unsigned long long>(c->ord_pbase),
                                     P_<unsigned long long>(c->ord_ibase), cap, ctr);
+    if (!(opts->mode & DPG_MODE_BALL_ONLY))
+      item_positions<<<(P + 255) / 256, 256, 0, st>>>(P, P_<unsigned long long>(c->ord_ibase), ctr,
+                                                      P_<uint32_t>(c->item_pos));
     if (N > 0) {
       nn_emit<<<(unsigned)((P * ((Wpad / 32 + kEmitGroups - 1) / kEmitGroups) + 7) / 8), 256, 0, st>>>(
           P, W, Wpad, P_<uint32_t>(c->mask), P_<uint32_t>(c->cnt), P_<unsigned long long>(c->pbase), cap,

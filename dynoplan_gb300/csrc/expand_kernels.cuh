@@ -523,6 +523,17 @@ static __global__ void __launch_bounds__(1024) scan_totals(int P, const int32_t 
   }
 }
 
+// item_pos[item] = the order position whose work items hold it (a thread per
+// position writes its run): the check kernel's item -> primitive lookup in
+// one load instead of a binary search over ord_ibase.  Nothing when the pairs
+// overflowed the capacity (no items then).
+static __global__ void item_positions(int P, const unsigned long long *ord_ibase, const DevCounters *ctr,
+                                      uint32_t *item_pos) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P || ctr->n_overflow) return;
+  for (unsigned long long it = ord_ibase[i]; it < ord_ibase[i + 1]; it++) item_pos[it] = (uint32_t)i;
+}
+
 // Pair lists from the primitive-major bitmask.  Warp per (primitive p, run of
 // kEmitGroups groups of 32 mask words; a group = 4 node tiles); lane = word.
 // The run's words are loaded up front (kEmitGroups loads in flight); for each
