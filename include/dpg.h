@@ -285,7 +285,9 @@ typedef struct dpg_tuning {
   int32_t check_blocks_per_sm; /* resident check blocks per SM, 0 = the occupancy maximum [0] */
   int32_t grid_min_nodes;      /* batches from this size scan the ball through the key grid [2048] */
   int32_t pipe_launches;       /* copy ranges of a host-output expand, 1..8 (check launches with
-                                  DPG_HOST_OUT_PIPELINED) [8] */
+                                  DPG_HOST_OUT_PIPELINED) [8]; each range a fraction of the one
+                                  before that the context adapts to its measured copy / check
+                                  time, and consecutive ranges under 16 MiB copied together */
   int32_t host_output;         /* DPG_HOST_OUT_* for host output arrays of a batch >= 2048 nodes
                                   [DPG_HOST_OUT_PROGRESS] */
 } dpg_tuning;
