@@ -316,7 +316,8 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
         "config": {"workload": wl.name, "primitives": wl.prims.P, "nodes_per_step": n,
-                   "obstacles": len(wl.env.obs_lo), "delta": wl.delta, "alpha": wl.alpha},
+                   "obstacles": len(wl.env.obs_lo), "delta": wl.delta, "alpha": wl.alpha,
+                   "outputs": "node, prim, verdict, first_invalid, end_state, min_gap (FP64)"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n} of {len(wl.nodes)} frontier states per step"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
