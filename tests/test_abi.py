@@ -5,7 +5,6 @@ import os
 import re
 import subprocess
 
-import numpy as np
 import pytest
 
 from dynoplan_gb300 import workloads as W

@@ -1,7 +1,6 @@
 """The search restatement's rule for a successor's g (its node's g when the
 batch was popped) against the reference's (the node's current g): one node
 per iteration gives identical searches (CPU, over the oracle's expand)."""
-import numpy as np
 import pytest
 
 import search_ref
