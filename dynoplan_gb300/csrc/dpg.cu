@@ -902,8 +902,8 @@ int dpg_expand(dpg_ctx *c, const dpg_expand_opts *opts, int64_t N, const double 
                                     P_<unsigned long long>(c->pbase), P_<unsigned long long>(c->ord_pbase),
                                     P_<unsigned long long>(c->ord_ibase), cap, ctr);
     if (!(opts->mode & DPG_MODE_BALL_ONLY))
-      item_positions<<<(P + 255) / 256, 256, 0, st>>>(P, P_<unsigned long long>(c->ord_ibase), ctr,
-                                                      P_<uint32_t>(c->item_pos));
+      item_positions<<<(unsigned)(((int64_t)P * 32 + 255) / 256), 256, 0, st>>>(
+          P, P_<unsigned long long>(c->ord_ibase), ctr, P_<uint32_t>(c->item_pos));
     if (N > 0) {
       nn_emit<<<(unsigned)((P * ((Wpad / 32 + kEmitGroups - 1) / kEmitGroups) + 7) / 8), 256, 0, st>>>(
           P, W, Wpad, P_<uint32_t>(c->mask), P_<uint32_t>(c->cnt), P_<unsigned long long>(c->pbase), cap,

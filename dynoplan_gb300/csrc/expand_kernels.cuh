@@ -523,15 +523,15 @@ static __global__ void __launch_bounds__(1024) scan_totals(int P, const int32_t 
   }
 }
 
-// item_pos[item] = the order position whose work items hold it (a thread per
-// position writes its run): the check kernel's item -> primitive lookup in
-// one load instead of a binary search over ord_ibase.  Nothing when the pairs
-// overflowed the capacity (no items then).
+// item_pos[item] = the order position whose work items hold it (a warp per
+// position writes its run, lane by lane): the check kernel's item ->
+// primitive lookup in one load instead of a binary search over ord_ibase.
+// Nothing when the pairs overflowed the capacity (no items then).
 static __global__ void item_positions(int P, const unsigned long long *ord_ibase, const DevCounters *ctr,
                                       uint32_t *item_pos) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (i >= P || ctr->n_overflow) return;
-  for (unsigned long long it = ord_ibase[i]; it < ord_ibase[i + 1]; it++) item_pos[it] = (uint32_t)i;
+  for (unsigned long long it = ord_ibase[i] + lane; it < ord_ibase[i + 1]; it += 32) item_pos[it] = (uint32_t)i;
 }
 
 // Pair lists from the primitive-major bitmask.  Warp per (primitive p, run of
